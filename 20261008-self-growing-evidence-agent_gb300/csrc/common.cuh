@@ -1,0 +1,139 @@
+// common.cuh -- shared declarations of the sgfim engine (host + device).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+// ------------------------------------------------------------------ errors
+// Device-side error codes written to the engine's error word.  A kernel that
+// gives up (bounded wait ran out, index out of range) records the first code
+// and the host turns it into SGFIM_EDEVICE.
+enum : uint32_t {
+    DEVERR_NONE = 0,
+    DEVERR_MBAR_TIMEOUT = 1,   // an mbarrier wait hit its iteration limit
+    DEVERR_BAD_ITEM = 2,       // a row index >= d reached a counting kernel
+    DEVERR_OVERFLOW = 3,       // an output buffer would overflow
+};
+
+#define SG_CUDA_TRY(expr)                                                       \
+    do {                                                                        \
+        cudaError_t e__ = (expr);                                               \
+        if (e__ != cudaSuccess) {                                               \
+            throw sg::CudaError(e__, #expr, __FILE__, __LINE__);               \
+        }                                                                       \
+    } while (0)
+
+namespace sg {
+
+struct CudaError {
+    cudaError_t code;
+    std::string what;
+    CudaError(cudaError_t c, const char *expr, const char *file, int line) : code(c) {
+        what = std::string(cudaGetErrorString(c)) + " at " + file + ":" + std::to_string(line) + " (" + expr + ")";
+    }
+};
+
+struct EngineError {
+    int code;
+    std::string what;
+    EngineError(int c, std::string w) : code(c), what(std::move(w)) {}
+};
+
+constexpr int kWarp = 32;
+constexpr uint32_t kMbarSpinLimit = 1u << 26;  // ~ seconds of polling; never unbounded
+
+// ------------------------------------------------------------------ device helpers
+__device__ __forceinline__ uint32_t popc64(uint64_t x) { return (uint32_t)__popcll(x); }
+
+__device__ __forceinline__ void set_device_error(uint32_t *err, uint32_t code) {
+    if (err) atomicCAS(err, 0u, code);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// One poll of the mbarrier phase; true once the phase with `parity` completed.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (and records DEVERR_MBAR_TIMEOUT) after
+// kMbarSpinLimit polls instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err) {
+    for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+    }
+    set_device_error(err, DEVERR_MBAR_TIMEOUT);
+    return false;
+}
+
+// 2-D tiled TMA load (global -> this CTA's shared memory), completion on bar.
+__device__ __forceinline__ void tma_load_2d(void *smem_dst, const CUtensorMap *map, int32_t x, int32_t y,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// 1-D bulk copy global -> shared (both 16-byte aligned, size multiple of 16).
+__device__ __forceinline__ void bulk_load_1d(void *smem_dst, const void *gsrc, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(gsrc)), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ uint4 ld_nc_v4(const void *p) {
+    uint4 r;
+    asm volatile("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t popc4(uint4 v) {
+    return __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+}
+
+__device__ __forceinline__ uint4 and4(uint4 a, uint4 b) {
+    return make_uint4(a.x & b.x, a.y & b.y, a.z & b.z, a.w & b.w);
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace sg

@@ -1,0 +1,98 @@
+// engine.h -- internal state of an sgfim handle.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sgfim.h"
+#include "kernels.h"
+
+namespace sg {
+
+// Device buffer with geometric growth; never shrinks until the handle closes.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void reserve(size_t want, cudaStream_t st);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Pinned host buffer with geometric growth.
+struct HostBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void reserve(size_t want);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct Dataset {
+    bool loaded = false;
+    uint64_t n_txn = 0;
+    uint32_t n_ids = 0;          // max id + 1
+    uint32_t n_present = 0;
+    uint32_t id_min = 0, id_max = 0;
+    uint64_t len_min = 0, len_max = 0;
+    double len_mean = 0;
+    std::vector<uint32_t> occ;   // occurrences per original id (duplicates counted)
+    std::vector<int32_t> o2d;    // original id -> dense row (-1 absent)
+    std::vector<uint32_t> d2o;   // dense row -> original id
+    std::vector<uint32_t> sup;   // dense row -> support (bitmap popcount)
+    uint32_t d = 0;              // bitmap rows
+    uint64_t n_words = 0;        // valid words per row (even)
+    uint64_t stride = 0;         // words per row (even)
+    DevBuf bitmaps;
+    DevBuf remap;                // int32 o2d on device (load_fimi/csr path)
+    DevBuf sup_dev;
+    CUtensorMap map{};
+    bool map_ok = false;
+    std::string source;          // file name or "<memory>"
+};
+
+// MLP scorer weights (device) for the learned frontier order.
+struct Scorer {
+    bool loaded = false;
+    uint32_t in_dim = 0, hidden = 0;
+    DevBuf w1, b1, w2, b2, w3, b3;
+};
+
+}  // namespace sg
+
+struct sgfim_handle {
+    int device = 0;
+    int n_sm = 0;
+    uint64_t hbm_budget = 0;
+    uint32_t wave_nodes = 0;
+    uint32_t flags = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    sg::Dataset ds;
+    sg::Scorer scorer;
+    // scratch
+    sg::DevBuf support_scratch, cand_ptr_dev, cand_items_dev, out_dev, dev_err;
+    sg::DevBuf cooc_scratch;
+    uint64_t launches = 0;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // phase timers: event quads recorded by timed calls, resolved by sgfim_phase_stats_get
+    struct Quad { cudaEvent_t e[4]; };
+    std::vector<Quad> timer_busy, timer_free;
+    sgfim_phase_stats pstats{};
+    cudaEvent_t *timer_quad();
+};
+
+namespace sg {
+int fail(sgfim_handle *h, int code, const std::string &msg);
+int check_device_error(sgfim_handle *h);
+// io.cpp
+int parse_fimi_file(const char *path, std::vector<uint64_t> &row_ptr, std::vector<uint32_t> &items, std::string &err);
+int write_tensorfim_file(const char *path, const sgfim_handle *h, const sgfim_result *r, const sgfim_tf_meta *m);
+int write_anyfim_file(const char *path, const sgfim_handle *h, sgfim_result *const *stages, const sgfim_af_meta *m);
+// miner.cu
+int mine_impl(sgfim_handle *h, const sgfim_mine_params *p, const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb,
+              void *user, sgfim_result **out);
+}  // namespace sg

@@ -1,0 +1,86 @@
+// kernels.h -- host-side launchers of the sgfim CUDA kernels.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sg {
+
+constexpr uint32_t kNoSlot = 0xffffffffu;
+
+// Counting modes of the streaming query kernel.
+enum QueryMode : int { QUERY_COUNT = 0, QUERY_ANY = 1 };
+
+// A batch of AND-popcount queries over row-major uint64 bitmaps.
+// Query q: popc(mask_q & AND_{i in items[ptr[q]..ptr[q+1])} rows[i]) over
+// words [0, n_words).  mask_q is arena + mask_slot[q] * arena_stride when
+// mask_slot is non-null and mask_slot[q] != kNoSlot, otherwise all ones.
+// In QUERY_ANY mode the result is only guaranteed to be 0 / non-zero.
+struct QueryBatch {
+    const uint64_t *rows = nullptr;
+    uint64_t row_stride = 0;        // words, even
+    uint64_t n_words = 0;           // valid words, even (padding words are zero)
+    uint32_t d = 0;                 // number of rows
+    const uint64_t *q_ptr = nullptr;   // n_q + 1
+    const uint32_t *q_items = nullptr;
+    const uint32_t *mask_slot = nullptr;  // optional, n_q
+    const uint64_t *arena = nullptr;
+    uint64_t arena_stride = 0;
+    uint64_t n_q = 0;
+    const uint64_t *n_q_device = nullptr;  // when set, the query count is read on the device
+    const uint32_t *q_index = nullptr;     // optional indirection: query j is q_index[j]
+    uint32_t *out = nullptr;
+    uint64_t empty_value = 0;       // result of an empty query without mask
+    int mode = QUERY_COUNT;
+};
+
+// Launchers (all asynchronous on `st`).
+void launch_transpose(const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn, const int32_t *remap,
+                      uint32_t d, uint64_t *bitmaps, uint64_t stride, uint32_t *counts, cudaStream_t st,
+                      int n_sm);
+void launch_row_popc(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t *counts,
+                     cudaStream_t st);
+void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm);
+
+// Batched candidate supports (config "support-1m" path).  Packs CSR candidates
+// into 16-byte records when every item fits 16 bits and k <= 8, runs the
+// shared-memory staged kernel on those and the streaming kernel on the rest.
+struct SupportPlan {
+    uint32_t threads = 1024;
+    uint32_t cands_per_cta = 0;    // 0 = derived from the SM count
+    uint32_t waves = 2;            // CTAs per SM over the whole grid (when cands_per_cta == 0)
+    bool force_stream = false;
+};
+struct SupportScratch {
+    // device scratch; sized by support_scratch_bytes()
+    void *base = nullptr;
+    size_t bytes = 0;
+};
+size_t support_scratch_bytes(uint64_t n_cand);
+// ev (optional, 4 events): recorded before prep, before the counting kernel,
+// after it, and after the >8-item tail.
+int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride,
+                         uint64_t n_txn, const uint64_t *cand_ptr, const uint32_t *cand_items, uint64_t n_cand,
+                         uint32_t *out, const SupportScratch &scratch, const SupportPlan &plan,
+                         const CUtensorMap *map, uint32_t *dev_err, cudaStream_t st, int n_sm,
+                         uint64_t *launches, cudaEvent_t *ev = nullptr);
+// Encode the 2-D tensor map used by the staged kernel (rows x words, u64).
+bool encode_bitmap_map(CUtensorMap *map, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
+                       uint64_t row_stride);
+size_t staged_smem_bytes(uint32_t d, uint32_t cands_per_cta);
+
+// Miner helpers.
+// mask(child c) = (parent_slot[c] != kNoSlot ? arena[parent_slot[c]] : ones) & AND rows(items[ptr[c]..ptr[c+1]))
+void launch_child_masks(uint64_t *arena, uint64_t arena_stride, uint64_t n_words, const uint64_t *rows,
+                        uint64_t row_stride, const uint64_t *ptr, const uint32_t *items, const uint32_t *parent_slot,
+                        const uint32_t *child_slot, uint32_t n, cudaStream_t st, int n_sm);
+void launch_pool_append(uint64_t *pool_rows, uint64_t pool_stride, const uint64_t *set_ptr,
+                        const uint32_t *set_items, uint64_t first_member, uint32_t n_sets, cudaStream_t st);
+
+// Co-occurrence (d x d) over the bitmap rows.
+int cooc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
+                int kind, cudaStream_t st, int n_sm, void *scratch, size_t scratch_bytes, uint64_t *launches);
+size_t cooc_scratch_bytes(uint32_t d, uint64_t n_words, int kind);
+
+}  // namespace sg

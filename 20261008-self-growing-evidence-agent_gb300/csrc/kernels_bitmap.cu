@@ -1,0 +1,501 @@
+// kernels_bitmap.cu -- bitmap build and AND-popcount support counting.
+//
+// Reference counterparts (paths relative to the reference project root):
+//   transpose_kernel   buildBitmap, code/engine_tensorfim/code/engine/src/kernel_bitmap.cu:342-380
+//                      (host scatter there; one CTA per transaction tile here)
+//   query_kernel       getResFrequencyCudaKernel, kernel_bitmap.cu:412-442 (one launch per
+//                      DFS node there; thousands of queries per launch here)
+//   k1_staged_kernel   the wave engine's maskBuild + BMMA counting, kernel_bmma.cu:603-768,
+//                      restated for arbitrary k-item candidates with the bitmap chunk staged
+//                      once per CTA in shared memory by TMA
+#include <algorithm>
+#include <cstdio>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+// ---------------------------------------------------------------- transpose
+// CSR transactions -> vertical bitmaps.  A CTA owns a tile of TW*64
+// transactions and builds the d x TW-word tile in shared memory with 32-bit
+// shared atomics, then writes each row's TW words (one 8*TW-byte run) and
+// adds the tile's popcounts to the singleton counts.
+__global__ void transpose_kernel(const uint64_t *__restrict__ row_ptr, const uint32_t *__restrict__ items,
+                                 uint64_t n_txn, const int32_t *__restrict__ remap, uint32_t n_ids, uint32_t d,
+                                 uint64_t *__restrict__ bm, uint64_t stride, uint32_t *__restrict__ counts,
+                                 uint32_t tw) {
+    extern __shared__ uint32_t tile[];  // d * 2*tw
+    const uint32_t tw32 = 2 * tw;
+    const uint64_t t0 = (uint64_t)blockIdx.x * tw * 64;
+    const uint64_t t1 = min(n_txn, t0 + (uint64_t)tw * 64);
+    for (uint32_t i = threadIdx.x; i < d * tw32; i += blockDim.x) tile[i] = 0;
+    __syncthreads();
+    for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const uint32_t local = (uint32_t)(t - t0);
+        for (uint64_t j = row_ptr[t]; j < row_ptr[t + 1]; ++j) {
+            const uint32_t id = items[j];
+            int32_t e = -1;
+            if (remap) {
+                if (id < n_ids) e = remap[id];
+            } else if (id < d) {
+                e = (int32_t)id;
+            }
+            if (e >= 0) atomicOr(&tile[(uint32_t)e * tw32 + (local >> 5)], 1u << (local & 31));
+        }
+    }
+    __syncthreads();
+    const uint64_t w0 = t0 / 64;
+    for (uint32_t i = threadIdx.x; i < d * tw; i += blockDim.x) {
+        const uint32_t e = i / tw, wl = i - e * tw;
+        const uint64_t gw = w0 + wl;
+        if (gw < stride) {
+            const uint64_t v = (uint64_t)tile[e * tw32 + 2 * wl] | ((uint64_t)tile[e * tw32 + 2 * wl + 1] << 32);
+            bm[(uint64_t)e * stride + gw] = v;
+        }
+    }
+    if (counts) {
+        for (uint32_t e = threadIdx.x; e < d; e += blockDim.x) {
+            uint32_t s = 0;
+            for (uint32_t k = 0; k < tw32; ++k) s += __popc(tile[e * tw32 + k]);
+            if (s) atomicAdd(&counts[e], s);
+        }
+    }
+}
+
+// Fallback for very wide item spaces: global 64-bit atomics, one thread per transaction.
+__global__ void transpose_global_kernel(const uint64_t *__restrict__ row_ptr, const uint32_t *__restrict__ items,
+                                        uint64_t n_txn, const int32_t *__restrict__ remap, uint32_t n_ids,
+                                        uint32_t d, unsigned long long *__restrict__ bm, uint64_t stride) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n_txn;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        for (uint64_t j = row_ptr[t]; j < row_ptr[t + 1]; ++j) {
+            const uint32_t id = items[j];
+            int32_t e = -1;
+            if (remap) {
+                if (id < n_ids) e = remap[id];
+            } else if (id < d) {
+                e = (int32_t)id;
+            }
+            if (e >= 0) atomicOr(&bm[(uint64_t)e * stride + (t >> 6)], 1ull << (t & 63));
+        }
+    }
+}
+
+__global__ void row_popc_kernel(const uint64_t *__restrict__ rows, uint64_t stride, uint64_t n_words, uint32_t d,
+                                uint32_t *__restrict__ counts) {
+    const uint32_t e = blockIdx.x;
+    if (e >= d) return;
+    uint32_t s = 0;
+    for (uint64_t w = threadIdx.x; w < n_words; w += blockDim.x) s += popc64(rows[e * stride + w]);
+    s = warp_sum(s);
+    __shared__ uint32_t part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) counts[e] = v;
+    }
+}
+
+void launch_transpose(const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn, const int32_t *remap,
+                      uint32_t d, uint64_t *bitmaps, uint64_t stride, uint32_t *counts, cudaStream_t st,
+                      int n_sm) {
+    (void)n_sm;
+    if (n_txn == 0 || d == 0) return;
+    // n_ids of the remap table is passed through `counts` sizing by the caller; the
+    // remap array covers every id that occurs (the caller builds it from the max id).
+    const uint32_t n_ids = 0xffffffffu;
+    const size_t budget = 160 * 1024;
+    uint32_t tw = 32;
+    while (tw > 1 && (size_t)d * tw * 8 > budget) tw >>= 1;
+    SG_CUDA_TRY(cudaMemsetAsync(bitmaps, 0, (size_t)d * stride * 8, st));
+    if ((size_t)d * tw * 8 > budget) {
+        transpose_global_kernel<<<1024, 256, 0, st>>>(row_ptr, items, n_txn, remap, n_ids, d,
+                                                      reinterpret_cast<unsigned long long *>(bitmaps), stride);
+        SG_CUDA_TRY(cudaGetLastError());
+        if (counts) launch_row_popc(bitmaps, stride, stride, d, counts, st);
+        return;
+    }
+    const size_t smem = (size_t)d * tw * 8;
+    SG_CUDA_TRY(cudaFuncSetAttribute(transpose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (counts) SG_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)d * 4, st));
+    const uint64_t tiles = (n_txn + (uint64_t)tw * 64 - 1) / ((uint64_t)tw * 64);
+    transpose_kernel<<<(unsigned)tiles, 512, smem, st>>>(row_ptr, items, n_txn, remap, n_ids, d, bitmaps, stride,
+                                                          counts, tw);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
+void launch_row_popc(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t *counts,
+                     cudaStream_t st) {
+    if (d == 0) return;
+    row_popc_kernel<<<d, 256, 0, st>>>(rows, stride, n_words, d, counts);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- streaming queries
+// One warp per query; each lane streams 16-byte words of the mask and of the
+// query's rows with non-coherent 128-bit loads, ANDs them and popcounts.
+__global__ void __launch_bounds__(256) query_kernel(QueryBatch qb) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t n_q = qb.n_q_device ? *qb.n_q_device : qb.n_q;
+    for (uint64_t j = warp; j < n_q; j += n_warps) {
+        const uint64_t q = qb.q_index ? qb.q_index[j] : j;
+        const uint64_t a = qb.q_ptr[q], b = qb.q_ptr[q + 1];
+        const uint64_t *mask = nullptr;
+        if (qb.mask_slot) {
+            const uint32_t s = qb.mask_slot[q];
+            if (s != kNoSlot) mask = qb.arena + (uint64_t)s * qb.arena_stride;
+        }
+        if (a == b && mask == nullptr) {
+            if (lane == 0) qb.out[q] = (uint32_t)qb.empty_value;
+            continue;
+        }
+        bool bad = false;
+        for (uint64_t i = a + lane; i < b; i += 32) bad |= qb.q_items[i] >= qb.d;
+        if (__any_sync(0xffffffffu, bad)) {
+            if (lane == 0) qb.out[q] = 0;
+            continue;
+        }
+        uint32_t acc = 0;
+        for (uint64_t base = 0; base < qb.n_words; base += 64) {
+            const uint64_t w = base + 2 * lane;
+            if (w < qb.n_words) {
+                uint4 v = mask ? ld_nc_v4(mask + w) : make_uint4(~0u, ~0u, ~0u, ~0u);
+                for (uint64_t i = a; i < b; ++i) v = and4(v, ld_nc_v4(qb.rows + (uint64_t)qb.q_items[i] * qb.row_stride + w));
+                acc += popc4(v);
+            }
+            if (qb.mode == QUERY_ANY && __any_sync(0xffffffffu, acc != 0)) break;
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) qb.out[q] = acc;
+    }
+}
+
+void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm) {
+    uint64_t blocks;
+    if (qb.n_q_device) {
+        blocks = (uint64_t)n_sm * 8;
+    } else {
+        if (qb.n_q == 0) return;
+        blocks = std::min<uint64_t>((qb.n_q + 7) / 8, (uint64_t)n_sm * 64);
+    }
+    query_kernel<<<(unsigned)blocks, 256, 0, st>>>(qb);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- staged batch supports
+// Candidate records: 8 x uint16 row ids; 0xffff marks unused slots and an
+// all-0xffff record marks a candidate whose support was written elsewhere.
+constexpr uint16_t kRecNone = 0xffffu;
+constexpr uint32_t kStagedRowsPerBox = 256;
+constexpr uint32_t kStagedWords = 16;   // words per row per chunk (128 bytes)
+
+__global__ void prep_records_kernel(const uint64_t *__restrict__ cand_ptr, const uint32_t *__restrict__ cand_items,
+                                    uint64_t n, uint32_t d, uint64_t n_txn, uint4 *__restrict__ recs,
+                                    uint32_t *__restrict__ ovf_list, unsigned long long *__restrict__ ovf_count,
+                                    uint32_t *__restrict__ out) {
+    for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = cand_ptr[c], b = cand_ptr[c + 1];
+        const uint64_t k = b - a;
+        uint32_t h[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+        if (k == 0) {
+            out[c] = (uint32_t)n_txn;
+        } else if (k > 8) {
+            const unsigned long long slot = atomicAdd(ovf_count, 1ull);
+            ovf_list[slot] = (uint32_t)c;
+        } else {
+            bool zero = false;
+            uint16_t it[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) it[i] = kRecNone;
+            for (uint64_t i = 0; i < k; ++i) {
+                const uint32_t x = cand_items[a + i];
+                if (x >= d) zero = true;
+                it[i] = (uint16_t)x;
+            }
+            if (zero) {
+                out[c] = 0;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) h[i] = (uint32_t)it[2 * i] | ((uint32_t)it[2 * i + 1] << 16);
+            }
+        }
+        recs[c] = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+}
+
+// 8-lane transpose-reduce: lane l (of an aligned group of 8) enters with
+// partials p[0..7] for 8 candidates and leaves with the group-wide sum of p[l].
+__device__ __forceinline__ uint32_t treduce8(const uint32_t (&p)[8], uint32_t l) {
+    uint32_t q[4], r[2];
+    const bool h4 = l & 4, h2 = l & 2, h1 = l & 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t send = h4 ? p[k] : p[k + 4];
+        const uint32_t keep = h4 ? p[k + 4] : p[k];
+        q[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t send = h2 ? q[k] : q[k + 2];
+        const uint32_t keep = h2 ? q[k + 2] : q[k];
+        r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    const uint32_t send = h1 ? r[0] : r[1];
+    const uint32_t keep = h1 ? r[1] : r[0];
+    return keep + __shfl_xor_sync(0xffffffffu, send, 1);
+}
+
+// Each CTA owns `cpc` consecutive candidates and sweeps the whole transaction
+// range in chunks of 16 words (1024 transactions).  Per chunk, TMA copies the
+// 128-byte slice of every bitmap row into shared memory (rows r*128 bytes
+// apart); a group of 8 lanes then evaluates one candidate at a time, each
+// lane ANDing a 16-byte piece of the k rows, so a warp reads 4 rows x 128
+// contiguous bytes per step (4 conflict-free wavefronts).  Partial popcounts
+// of 8 candidates are transpose-reduced into one register per lane, which
+// accumulates across chunks: each support is written once, at the end.
+template <int THREADS, int SMAX>
+__global__ void __launch_bounds__(THREADS, 1)
+    k1_staged_kernel(const __grid_constant__ CUtensorMap bm_map, uint32_t n_boxes, uint64_t n_words,
+                     const uint4 *__restrict__ recs, uint64_t n_cand, uint32_t cpc, uint32_t *__restrict__ out,
+                     uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr uint32_t G = THREADS / 8;             // groups of 8 lanes
+    uint8_t *chunk = smem;                           // n_boxes * 256 rows * 128 B
+    const uint32_t chunk_bytes = n_boxes * kStagedRowsPerBox * kStagedWords * 8;
+    uint4 *rec_s = reinterpret_cast<uint4 *>(smem + chunk_bytes);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + chunk_bytes + (size_t)cpc * 16);
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t g = tid >> 3, l = tid & 7;
+    const uint64_t base = (uint64_t)blockIdx.x * cpc;
+    if (base >= n_cand) return;
+    const uint64_t left = n_cand - base;
+    const uint32_t ncta = left < cpc ? (uint32_t)left : cpc;
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    for (uint32_t i = tid; i < ncta; i += THREADS) rec_s[i] = recs[base + i];
+    __syncthreads();
+
+    uint32_t acc[SMAX];
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) acc[s] = 0;
+    const uint32_t n_sets = (ncta + 8 * G - 1) / (8 * G);
+    const uint64_t n_chunks = (n_words + kStagedWords - 1) / kStagedWords;
+    uint32_t phase = 0;
+    for (uint64_t ch = 0; ch < n_chunks; ++ch) {
+        if (tid == 0) {
+            mbar_arrive_expect_tx(bar, chunk_bytes);
+            for (uint32_t b = 0; b < n_boxes; ++b)
+                tma_load_2d(chunk + (size_t)b * kStagedRowsPerBox * kStagedWords * 8, &bm_map,
+                            (int32_t)(ch * kStagedWords), (int32_t)(b * kStagedRowsPerBox), bar);
+        }
+        const bool ok = mbar_wait_bounded(bar, phase, err);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            // give in-flight copies one more bounded chance to land before leaving
+            mbar_wait_bounded(bar, phase ^ 1, err);
+            return;
+        }
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s) {
+            if ((uint32_t)s < n_sets) {
+                uint32_t p[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const uint32_t c = ((uint32_t)s * 8 + j) * G + g;
+                    uint32_t v = 0;
+                    if (c < ncta) {
+                        const uint4 r = rec_s[c];
+                        const uint32_t h[4] = {r.x, r.y, r.z, r.w};
+                        uint32_t it0 = h[0] & 0xffffu;
+                        if (it0 != kRecNone) {
+                            uint4 m = *reinterpret_cast<const uint4 *>(chunk + (size_t)it0 * 128 + l * 16);
+#pragma unroll
+                            for (int k = 1; k < 8; ++k) {
+                                const uint32_t it = (h[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+                                if (it == kRecNone) break;
+                                m = and4(m, *reinterpret_cast<const uint4 *>(chunk + (size_t)it * 128 + l * 16));
+                            }
+                            v = popc4(m);
+                        }
+                    }
+                    p[j] = v;
+                }
+                acc[s] += treduce8(p, l);
+            }
+        }
+        __syncthreads();  // every group is done with this chunk before TMA overwrites it
+    }
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) {
+        const uint32_t c = ((uint32_t)s * 8 + l) * G + g;
+        if ((uint32_t)s < n_sets && c < ncta) {
+            const uint32_t it0 = rec_s[c].x & 0xffffu;
+            if (it0 != kRecNone) out[base + c] = acc[s];
+        }
+    }
+}
+
+constexpr int kStagedThreads = 1024;
+constexpr int kStagedSmax = 8;
+constexpr uint32_t kStagedMaxCpc = kStagedThreads / 8 * 8 * kStagedSmax;  // 8192
+
+size_t staged_smem_bytes(uint32_t d, uint32_t cpc) {
+    const uint32_t n_boxes = (d + kStagedRowsPerBox - 1) / kStagedRowsPerBox;
+    return (size_t)n_boxes * kStagedRowsPerBox * kStagedWords * 8 + (size_t)cpc * 16 + 64;
+}
+
+bool encode_bitmap_map(CUtensorMap *map, const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride) {
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return false;
+        fn = reinterpret_cast<EncodeFn>(p);
+    }
+    if ((reinterpret_cast<uintptr_t>(bitmaps) & 15) || (row_stride & 1)) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)n_words, (cuuint64_t)d};
+    cuuint64_t strides[1] = {(cuuint64_t)row_stride * 8};
+    cuuint32_t box[2] = {kStagedWords, kStagedRowsPerBox};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<uint64_t *>(bitmaps), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+size_t support_scratch_bytes(uint64_t n_cand) {
+    return align_up(n_cand * 16, 256) + align_up(n_cand * 4, 256) + 256;
+}
+
+int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride,
+                         uint64_t n_txn, const uint64_t *cand_ptr, const uint32_t *cand_items, uint64_t n_cand,
+                         uint32_t *out, const SupportScratch &scratch, const SupportPlan &plan,
+                         const CUtensorMap *map, uint32_t *dev_err, cudaStream_t st, int n_sm, uint64_t *launches,
+                         cudaEvent_t *ev) {
+    if (n_cand == 0) return 0;
+    auto mark = [&](int i) {
+        if (ev) SG_CUDA_TRY(cudaEventRecord(ev[i], st));
+    };
+    const uint64_t n_words_even = (n_words + 1) & ~1ull;
+    bool staged = !plan.force_stream && map != nullptr && d <= 65535 && d > 0;
+    uint32_t cpc = plan.cands_per_cta;
+    if (staged) {
+        if (cpc == 0) {
+            const uint64_t ctas = (uint64_t)n_sm * std::max<uint32_t>(1, plan.waves);
+            cpc = (uint32_t)std::min<uint64_t>(kStagedMaxCpc, (n_cand + ctas - 1) / ctas);
+            cpc = std::max<uint32_t>(cpc, 1);
+        }
+        cpc = std::min(cpc, kStagedMaxCpc);
+        while (cpc > 1 && staged_smem_bytes(d, cpc) > 227 * 1024) cpc = cpc * 3 / 4;
+        if (staged_smem_bytes(d, cpc) > 227 * 1024) staged = false;
+    }
+    if (!staged) {
+        QueryBatch qb;
+        qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;
+        qb.q_ptr = cand_ptr; qb.q_items = cand_items; qb.n_q = n_cand; qb.out = out; qb.empty_value = n_txn;
+        mark(0);
+        mark(1);
+        launch_queries(qb, st, n_sm);
+        mark(2);
+        mark(3);
+        if (launches) *launches += 1;
+        return 0;
+    }
+    if (scratch.bytes < support_scratch_bytes(n_cand)) return -1;
+    uint8_t *sb = static_cast<uint8_t *>(scratch.base);
+    uint4 *recs = reinterpret_cast<uint4 *>(sb);
+    uint32_t *ovf = reinterpret_cast<uint32_t *>(sb + align_up(n_cand * 16, 256));
+    unsigned long long *ovf_n =
+        reinterpret_cast<unsigned long long *>(sb + align_up(n_cand * 16, 256) + align_up(n_cand * 4, 256));
+    mark(0);
+    SG_CUDA_TRY(cudaMemsetAsync(ovf_n, 0, 8, st));
+    const unsigned prep_blocks = (unsigned)std::min<uint64_t>((n_cand + 255) / 256, (uint64_t)n_sm * 16);
+    prep_records_kernel<<<prep_blocks, 256, 0, st>>>(cand_ptr, cand_items, n_cand, d, n_txn, recs, ovf, ovf_n, out);
+    SG_CUDA_TRY(cudaGetLastError());
+    const uint32_t n_boxes = (d + kStagedRowsPerBox - 1) / kStagedRowsPerBox;
+    const size_t smem = staged_smem_bytes(d, cpc);
+    auto kern = k1_staged_kernel<kStagedThreads, kStagedSmax>;
+    SG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const uint64_t ctas = (n_cand + cpc - 1) / cpc;
+    mark(1);
+    kern<<<(unsigned)ctas, kStagedThreads, smem, st>>>(*map, n_boxes, n_words_even, recs, n_cand, cpc, out, dev_err);
+    SG_CUDA_TRY(cudaGetLastError());
+    mark(2);
+    // candidates with more than 8 items
+    QueryBatch qb;
+    qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;
+    qb.q_ptr = cand_ptr; qb.q_items = cand_items; qb.n_q_device = reinterpret_cast<const uint64_t *>(ovf_n);
+    qb.q_index = ovf; qb.out = out; qb.empty_value = n_txn;
+    launch_queries(qb, st, n_sm);
+    mark(3);
+    if (launches) *launches += 3;
+    return 0;
+}
+
+// ---------------------------------------------------------------- miner helpers
+__global__ void child_mask_kernel(uint64_t *__restrict__ arena, uint64_t astride, uint64_t n_words,
+                                  const uint64_t *__restrict__ rows, uint64_t rstride, const uint64_t *__restrict__ ptr,
+                                  const uint32_t *__restrict__ items, const uint32_t *__restrict__ parent_slot,
+                                  const uint32_t *__restrict__ child_slot, uint32_t n) {
+    const uint64_t n_vec = n_words / 2;
+    const uint64_t total = (uint64_t)n * n_vec;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(i / n_vec);
+        const uint64_t v = i - (uint64_t)c * n_vec;
+        const uint32_t ps = parent_slot[c];
+        uint4 r = make_uint4(~0u, ~0u, ~0u, ~0u);
+        if (ps != kNoSlot) r = *reinterpret_cast<const uint4 *>(arena + (uint64_t)ps * astride + 2 * v);
+        for (uint64_t j = ptr[c]; j < ptr[c + 1]; ++j) r = and4(r, ld_nc_v4(rows + (uint64_t)items[j] * rstride + 2 * v));
+        *reinterpret_cast<uint4 *>(arena + (uint64_t)child_slot[c] * astride + 2 * v) = r;
+    }
+}
+
+void launch_child_masks(uint64_t *arena, uint64_t arena_stride, uint64_t n_words, const uint64_t *rows,
+                        uint64_t row_stride, const uint64_t *ptr, const uint32_t *items, const uint32_t *parent_slot,
+                        const uint32_t *child_slot, uint32_t n, cudaStream_t st, int n_sm) {
+    if (n == 0) return;
+    const uint64_t total = (uint64_t)n * (n_words / 2);
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)n_sm * 32);
+    child_mask_kernel<<<blocks, 256, 0, st>>>(arena, arena_stride, n_words, rows, row_stride, ptr, items, parent_slot,
+                                              child_slot, n);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
+__global__ void pool_append_kernel(unsigned long long *__restrict__ pool, uint64_t pstride,
+                                   const uint64_t *__restrict__ set_ptr, const uint32_t *__restrict__ set_items,
+                                   uint64_t first, uint32_t n_sets) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_sets; s += gridDim.x * blockDim.x) {
+        const uint64_t m = first + s;
+        for (uint64_t i = set_ptr[s]; i < set_ptr[s + 1]; ++i)
+            atomicOr(&pool[(uint64_t)set_items[i] * pstride + (m >> 6)], 1ull << (m & 63));
+    }
+}
+
+void launch_pool_append(uint64_t *pool_rows, uint64_t pool_stride, const uint64_t *set_ptr, const uint32_t *set_items,
+                        uint64_t first_member, uint32_t n_sets, cudaStream_t st) {
+    if (n_sets == 0) return;
+    const unsigned blocks = std::min<unsigned>((n_sets + 255) / 256, 1024);
+    pool_append_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<unsigned long long *>(pool_rows), pool_stride,
+                                               set_ptr, set_items, first_member, n_sets);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
+}  // namespace sg

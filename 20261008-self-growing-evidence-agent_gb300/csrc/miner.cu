@@ -1,0 +1,552 @@
+// miner.cu -- exact MFI search driven from the host in device waves.
+//
+// Reference counterparts: the engines' task-stack DFS (kernel_bitmap.cu:841-894,
+// kernel_bmma.cu:875-910 "wave engine", AnytimeMining/kernel.cu:862-899) and the
+// oracle miner mine_mfi (code/pipeline/skab_spike.py:84-135).  The reference
+// engines enumerate every frequent itemset; this engine searches the same
+// set-enumeration tree with the pruning rules of an exact MFI miner:
+//
+//   node (H, T):   s_e = sup(H u {e}) for e in T, counted on the device from H's
+//                  tidset mask (one batched launch per wave of nodes)
+//   PEP:           e with s_e == sup(H) joins H (same tidset)
+//   order:         the remaining frequent tail F sorted by ascending support
+//   leaf:          F empty -> H is a candidate unless a pool member contains it
+//   HUT:           H u F contained in a pool member -> no new MFI below
+//   FHUT:          sup(H u F) >= thr -> H u F is the subtree's only candidate
+//   children:      H u {f_i} with tail f_{i+1..}, masks built on the device
+//
+// The pool of candidates lives on the device as a vertical bitmap (one bit
+// per candidate in every item's row), so "is Q contained in a candidate" is an
+// AND-popcount query over the pool rows -- the same kernel as support counting.
+// Candidates emitted in one wave are not tested against each other, so the
+// final maximality filter counts, for every candidate, the pool members that
+// contain it; exactly one (itself) means the candidate is maximal.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <queue>
+
+#include "common.cuh"
+#include "engine.h"
+
+namespace sg {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct MNode {
+    std::vector<uint32_t> head;  // dense ids
+    std::vector<uint32_t> tail;  // dense ids, search order
+    uint32_t sup = 0;
+    uint32_t slot = kNoSlot;     // tidset mask slot; kNoSlot = AND of head rows
+    float prio = 0.f;
+};
+
+struct QuerySet {
+    std::vector<uint64_t> ptr{0};
+    std::vector<uint32_t> items;
+    std::vector<uint32_t> slot;
+    void clear() { ptr.assign(1, 0); items.clear(); slot.clear(); }
+    size_t size() const { return slot.size(); }
+    void add(const uint32_t *it, size_t k, uint32_t s) {
+        items.insert(items.end(), it, it + k);
+        ptr.push_back(items.size());
+        slot.push_back(s);
+    }
+};
+
+class Miner {
+  public:
+    Miner(sgfim_handle *h, const sgfim_mine_params &p) : h_(h), ds_(h->ds), p_(p) {}
+    ~Miner() {
+        arena_.release(); pool_.release();
+        dq_ptr_.release(); dq_items_.release(); dq_slot_.release(); dq_out_.release();
+        hq_ptr_.release(); hq_items_.release(); hq_slot_.release(); hq_out_.release();
+    }
+
+    int run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out);
+
+  private:
+    sgfim_handle *h_;
+    Dataset &ds_;
+    sgfim_mine_params p_;
+    uint32_t thr_ = 1;
+    Clock::time_point t0_;
+    // tidset masks
+    DevBuf arena_;
+    uint64_t slot_words_ = 0;
+    std::vector<uint32_t> free_slots_;
+    // device pool (rows = items, one bit per candidate)
+    DevBuf pool_;
+    uint64_t pool_words_ = 0;   // words per pool row (capacity / 64)
+    uint64_t pool_n_ = 0;       // members in the device pool
+    // candidates (host)
+    std::vector<uint64_t> cptr_{0};
+    std::vector<uint32_t> citems_;
+    std::vector<uint32_t> csup_;
+    std::vector<double> ctime_;
+    // query staging
+    DevBuf dq_ptr_, dq_items_, dq_slot_, dq_out_;
+    HostBuf hq_ptr_, hq_items_, hq_slot_, hq_out_;
+    uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
+
+    double elapsed() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
+    uint32_t alloc_slot() {
+        if (free_slots_.empty()) return kNoSlot;
+        uint32_t s = free_slots_.back();
+        free_slots_.pop_back();
+        return s;
+    }
+    void run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
+                     int mode, std::vector<uint32_t> &out);
+    void pool_reserve(uint64_t members);
+    void emit(const std::vector<uint32_t> &set, uint32_t sup);
+    void flush_pool(uint64_t from);
+    int finish(sgfim_result **out);
+};
+
+void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
+                        int mode, std::vector<uint32_t> &out) {
+    const size_t n = qs.size();
+    out.assign(n, 0);
+    if (n == 0) return;
+    cudaStream_t st = h_->stream;
+    hq_ptr_.reserve((n + 1) * 8);
+    hq_items_.reserve(std::max<size_t>(qs.items.size(), 1) * 4);
+    hq_slot_.reserve(n * 4);
+    hq_out_.reserve(n * 4);
+    memcpy(hq_ptr_.ptr, qs.ptr.data(), (n + 1) * 8);
+    if (!qs.items.empty()) memcpy(hq_items_.ptr, qs.items.data(), qs.items.size() * 4);
+    memcpy(hq_slot_.ptr, qs.slot.data(), n * 4);
+    dq_ptr_.reserve((n + 1) * 8, st);
+    dq_items_.reserve(std::max<size_t>(qs.items.size(), 1) * 4, st);
+    dq_slot_.reserve(n * 4, st);
+    dq_out_.reserve(n * 4, st);
+    SG_CUDA_TRY(cudaMemcpyAsync(dq_ptr_.ptr, hq_ptr_.ptr, (n + 1) * 8, cudaMemcpyHostToDevice, st));
+    if (!qs.items.empty())
+        SG_CUDA_TRY(cudaMemcpyAsync(dq_items_.ptr, hq_items_.ptr, qs.items.size() * 4, cudaMemcpyHostToDevice, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(dq_slot_.ptr, hq_slot_.ptr, n * 4, cudaMemcpyHostToDevice, st));
+    QueryBatch qb;
+    qb.rows = rows; qb.row_stride = stride; qb.n_words = n_words; qb.d = d;
+    qb.q_ptr = dq_ptr_.as<uint64_t>(); qb.q_items = dq_items_.as<uint32_t>();
+    qb.mask_slot = dq_slot_.as<uint32_t>(); qb.arena = arena_.as<uint64_t>(); qb.arena_stride = slot_words_;
+    qb.n_q = n; qb.out = dq_out_.as<uint32_t>(); qb.empty_value = ds_.n_txn; qb.mode = mode;
+    launch_queries(qb, st, h_->n_sm);
+    ++launches_;
+    SG_CUDA_TRY(cudaMemcpyAsync(hq_out_.ptr, dq_out_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(out.data(), hq_out_.ptr, n * 4);
+}
+
+void Miner::pool_reserve(uint64_t members) {
+    const uint64_t need_words = ((members + 63) / 64 + 1) & ~1ull;
+    if (need_words <= pool_words_) return;
+    uint64_t nw = std::max<uint64_t>(need_words, std::max<uint64_t>(pool_words_ * 2, 1024));
+    nw = (nw + 1) & ~1ull;
+    void *np = nullptr;
+    SG_CUDA_TRY(cudaMalloc(&np, (size_t)ds_.d * nw * 8));
+    SG_CUDA_TRY(cudaMemsetAsync(np, 0, (size_t)ds_.d * nw * 8, h_->stream));
+    if (pool_.ptr && pool_words_)
+        SG_CUDA_TRY(cudaMemcpy2DAsync(np, nw * 8, pool_.ptr, pool_words_ * 8, pool_words_ * 8, ds_.d,
+                                      cudaMemcpyDeviceToDevice, h_->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(h_->stream));
+    pool_.release();
+    pool_.ptr = np;
+    pool_.bytes = (size_t)ds_.d * nw * 8;
+    pool_words_ = nw;
+}
+
+void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup) {
+    std::vector<uint32_t> s(set);
+    std::sort(s.begin(), s.end());
+    citems_.insert(citems_.end(), s.begin(), s.end());
+    cptr_.push_back(citems_.size());
+    csup_.push_back(sup);
+    ctime_.push_back(elapsed());
+}
+
+// Append candidates [from, n) to the device pool.
+void Miner::flush_pool(uint64_t from) {
+    const uint64_t n = csup_.size();
+    if (from >= n) return;
+    pool_reserve(n);
+    const uint32_t cnt = (uint32_t)(n - from);
+    std::vector<uint64_t> lp(cnt + 1);
+    for (uint32_t i = 0; i <= cnt; ++i) lp[i] = cptr_[from + i] - cptr_[from];
+    const uint64_t ni = lp[cnt];
+    DevBuf dp, di;
+    dp.reserve((cnt + 1) * 8, h_->stream);
+    di.reserve(std::max<uint64_t>(ni, 1) * 4, h_->stream);
+    SG_CUDA_TRY(cudaMemcpyAsync(dp.ptr, lp.data(), (cnt + 1) * 8, cudaMemcpyHostToDevice, h_->stream));
+    SG_CUDA_TRY(cudaMemcpyAsync(di.ptr, citems_.data() + cptr_[from], ni * 4, cudaMemcpyHostToDevice, h_->stream));
+    launch_pool_append(pool_.as<uint64_t>(), pool_words_, dp.as<uint64_t>(), di.as<uint32_t>(), from, cnt,
+                       h_->stream);
+    ++launches_;
+    SG_CUDA_TRY(cudaStreamSynchronize(h_->stream));
+    dp.release();
+    di.release();
+    pool_n_ = n;
+}
+
+int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out) {
+    *out = nullptr;
+    if (!ds_.loaded) return fail(h_, SGFIM_ESTATE, "no dataset loaded");
+    if (p_.min_count < 1) return fail(h_, SGFIM_EINVAL, "min_count must be >= 1");
+    if (p_.order == SGFIM_ORDER_LEARNED && !h_->scorer.loaded)
+        return fail(h_, SGFIM_ESTATE, "learned order requested but no scorer loaded");
+    thr_ = p_.min_count;
+    t0_ = Clock::now();
+    cudaStream_t st = h_->stream;
+    const uint32_t d = ds_.d;
+
+    // frequent items, ascending support (ties ascending id)
+    std::vector<uint32_t> freq;
+    for (uint32_t e = 0; e < d; ++e)
+        if (ds_.sup[e] >= thr_) freq.push_back(e);
+    std::stable_sort(freq.begin(), freq.end(), [&](uint32_t a, uint32_t b) { return ds_.sup[a] < ds_.sup[b]; });
+
+    // mask arena
+    slot_words_ = ds_.stride;
+    const uint64_t slot_bytes = slot_words_ * 8;
+    uint64_t budget = h_->hbm_budget / 4;
+    uint64_t max_slots = std::min<uint64_t>(1u << 20, budget / std::max<uint64_t>(slot_bytes, 1));
+    max_slots = std::min<uint64_t>(max_slots, std::max<uint64_t>(4096, (uint64_t)freq.size() * 64));
+    if (max_slots < 64) max_slots = 64;
+    arena_.reserve(max_slots * slot_bytes, st);
+    free_slots_.resize(max_slots);
+    for (uint64_t i = 0; i < max_slots; ++i) free_slots_[i] = (uint32_t)(max_slots - 1 - i);
+    pool_reserve(65536);
+
+    const uint64_t qmax = 1u << 17;                         // queries per wave
+    const uint64_t nmax = h_->wave_nodes ? h_->wave_nodes : 8192;  // nodes per wave
+    std::vector<MNode> stack;
+    {
+        MNode root;
+        root.tail = freq;
+        root.sup = (uint32_t)ds_.n_txn;
+        if (!freq.empty()) stack.push_back(std::move(root));
+    }
+    uint32_t next_ck = 0;
+    std::vector<MNode> wave;
+    QuerySet qs, qpool, qfhut, qchild;
+    std::vector<uint32_t> counts, pool_hit, fhut_cnt;
+    int status = SGFIM_OK;
+
+    while (!stack.empty()) {
+        // ---- pop a wave
+        wave.clear();
+        uint64_t nq = 0;
+        while (!stack.empty() && wave.size() < nmax) {
+            const uint64_t w = stack.back().tail.size();
+            if (!wave.empty() && nq + w > qmax) break;
+            nq += w;
+            wave.push_back(std::move(stack.back()));
+            stack.pop_back();
+        }
+        ++waves_;
+        nodes_ += wave.size();
+        // ---- phase A: s_e for every tail item
+        qs.clear();
+        std::vector<uint32_t> tmp;
+        for (const MNode &nd : wave) {
+            for (uint32_t e : nd.tail) {
+                if (nd.slot != kNoSlot) {
+                    qs.add(&e, 1, nd.slot);
+                } else {
+                    tmp.assign(nd.head.begin(), nd.head.end());
+                    tmp.push_back(e);
+                    qs.add(tmp.data(), tmp.size(), kNoSlot);
+                }
+            }
+        }
+        run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts);
+        // ---- phase B: PEP, ordering, pool and FHUT queries
+        struct Work {
+            std::vector<uint32_t> head;           // after PEP
+            std::vector<std::pair<uint32_t, uint32_t>> f;  // (support, item) ascending
+            int kind = 0;                         // 0 leaf, 1 internal
+            size_t pool_q = 0, fhut_q = 0;
+        };
+        std::vector<Work> work(wave.size());
+        qpool.clear();
+        qfhut.clear();
+        size_t off = 0;
+        for (size_t i = 0; i < wave.size(); ++i) {
+            MNode &nd = wave[i];
+            Work &wk = work[i];
+            wk.head = nd.head;
+            for (size_t j = 0; j < nd.tail.size(); ++j) {
+                const uint32_t s = counts[off + j];
+                if (s < thr_) continue;
+                if (s == nd.sup) wk.head.push_back(nd.tail[j]);
+                else wk.f.emplace_back(s, nd.tail[j]);
+            }
+            off += nd.tail.size();
+            std::stable_sort(wk.f.begin(), wk.f.end(),
+                             [](const std::pair<uint32_t, uint32_t> &a, const std::pair<uint32_t, uint32_t> &b) {
+                                 return a.first < b.first || (a.first == b.first && a.second < b.second);
+                             });
+            if (wk.f.empty()) {
+                wk.kind = 0;
+                wk.pool_q = qpool.size();
+                qpool.add(wk.head.data(), wk.head.size(), kNoSlot);
+            } else {
+                wk.kind = 1;
+                tmp.assign(wk.head.begin(), wk.head.end());
+                for (auto &pr : wk.f) tmp.push_back(pr.second);
+                wk.pool_q = qpool.size();
+                qpool.add(tmp.data(), tmp.size(), kNoSlot);
+                wk.fhut_q = qfhut.size();
+                if (nd.slot != kNoSlot) {
+                    qfhut.add(tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
+                } else {
+                    qfhut.add(tmp.data(), tmp.size(), kNoSlot);
+                }
+            }
+        }
+        if (pool_n_ > 0) {
+            const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
+            run_queries(qpool, pool_.as<uint64_t>(), pool_words_, pw, d, QUERY_ANY, pool_hit);
+        } else {
+            pool_hit.assign(qpool.size(), 0);
+        }
+        run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt);
+        // ---- phase C: emit candidates, expand children
+        const uint64_t pool_before = csup_.size();
+        qchild.clear();
+        std::vector<uint32_t> child_parent, child_slot;
+        std::vector<MNode> children_rev;
+        for (size_t i = 0; i < wave.size(); ++i) {
+            MNode &nd = wave[i];
+            Work &wk = work[i];
+            if (wk.kind == 0) {
+                if (!wk.head.empty() && pool_hit[wk.pool_q] == 0) emit(wk.head, nd.sup);
+                continue;
+            }
+            if (pool_hit[wk.pool_q] != 0) continue;  // HUT
+            if (fhut_cnt[wk.fhut_q] >= thr_) {       // FHUT
+                tmp.assign(wk.head.begin(), wk.head.end());
+                for (auto &pr : wk.f) tmp.push_back(pr.second);
+                emit(tmp, fhut_cnt[wk.fhut_q]);
+                continue;
+            }
+            // children in search order; pushed in reverse so the first is popped first
+            const size_t nf = wk.f.size();
+            std::vector<MNode> kids(nf);
+            for (size_t j = 0; j < nf; ++j) {
+                MNode &c = kids[j];
+                c.head = wk.head;
+                c.head.push_back(wk.f[j].second);
+                c.sup = wk.f[j].first;
+                c.tail.reserve(nf - j - 1);
+                for (size_t k = j + 1; k < nf; ++k) c.tail.push_back(wk.f[k].second);
+                if (c.tail.empty()) {
+                    // a child without tail is a leaf: its own wave will test it against the pool
+                    c.slot = kNoSlot;
+                    continue;
+                }
+                c.slot = alloc_slot();
+                if (c.slot != kNoSlot) {
+                    if (nd.slot != kNoSlot) {
+                        const uint32_t e = wk.f[j].second;
+                        qchild.add(&e, 1, nd.slot);
+                    } else {
+                        qchild.add(c.head.data(), c.head.size(), kNoSlot);
+                    }
+                    child_slot.push_back(c.slot);
+                }
+            }
+            for (size_t j = nf; j-- > 0;) children_rev.push_back(std::move(kids[j]));
+        }
+        // child masks: mask(child) = mask(parent) & AND rows(list)
+        if (qchild.size()) {
+            dq_ptr_.reserve((qchild.size() + 1) * 8, st);
+            // reuse the generic staging: child masks use the query arrays + a slot list
+            const size_t n = qchild.size();
+            std::vector<uint32_t> pslot(qchild.slot);
+            DevBuf dptr, ditems, dps, dcs;
+            dptr.reserve((n + 1) * 8, st);
+            ditems.reserve(std::max<size_t>(qchild.items.size(), 1) * 4, st);
+            dps.reserve(n * 4, st);
+            dcs.reserve(n * 4, st);
+            SG_CUDA_TRY(cudaMemcpyAsync(dptr.ptr, qchild.ptr.data(), (n + 1) * 8, cudaMemcpyHostToDevice, st));
+            SG_CUDA_TRY(cudaMemcpyAsync(ditems.ptr, qchild.items.data(), qchild.items.size() * 4,
+                                        cudaMemcpyHostToDevice, st));
+            SG_CUDA_TRY(cudaMemcpyAsync(dps.ptr, pslot.data(), n * 4, cudaMemcpyHostToDevice, st));
+            SG_CUDA_TRY(cudaMemcpyAsync(dcs.ptr, child_slot.data(), n * 4, cudaMemcpyHostToDevice, st));
+            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(), ds_.stride,
+                               dptr.as<uint64_t>(), ditems.as<uint32_t>(), dps.as<uint32_t>(), dcs.as<uint32_t>(),
+                               (uint32_t)n, st, h_->n_sm);
+            ++launches_;
+            SG_CUDA_TRY(cudaStreamSynchronize(st));
+            dptr.release(); ditems.release(); dps.release(); dcs.release();
+        }
+        // parents' masks are no longer needed
+        for (MNode &nd : wave)
+            if (nd.slot != kNoSlot) free_slots_.push_back(nd.slot);
+        for (MNode &c : children_rev) stack.push_back(std::move(c));
+        flush_pool(pool_before);
+        // ---- checkpoints, limits
+        const double el = elapsed();
+        while (next_ck < n_ckpt && el >= ckpts[next_ck]) {
+            if (cb) {
+                std::vector<uint64_t> op(cptr_);
+                std::vector<uint32_t> oi(citems_.size());
+                for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
+                sgfim_checkpoint ck;
+                ck.t_s = ckpts[next_ck];
+                ck.elapsed_s = el;
+                ck.n_emitted = csup_.size();
+                ck.set_ptr = op.data();
+                ck.items = oi.data();
+                ck.support = csup_.data();
+                ck.nodes = nodes_;
+                if (cb(user, &ck) != 0) { status = SGFIM_ECANCELED; break; }
+            }
+            ++next_ck;
+        }
+        if (status != SGFIM_OK) break;
+        if (p_.time_limit_s > 0 && el > p_.time_limit_s) { status = SGFIM_ETIMEDOUT; break; }
+        if (p_.node_limit && nodes_ > p_.node_limit) { status = SGFIM_ENOMEM; break; }
+    }
+    if (status != SGFIM_OK) {
+        h_->launches += launches_;
+        return fail(h_, status, status == SGFIM_ECANCELED ? "stopped by checkpoint callback"
+                                : status == SGFIM_ETIMEDOUT ? "time limit expired"
+                                                            : "node limit exceeded");
+    }
+    // remaining checkpoints fire once the search is complete
+    if (cb) {
+        const double el = elapsed();
+        std::vector<uint32_t> oi(citems_.size());
+        for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
+        for (; next_ck < n_ckpt; ++next_ck) {
+            sgfim_checkpoint ck;
+            ck.t_s = ckpts[next_ck];
+            ck.elapsed_s = el;
+            ck.n_emitted = csup_.size();
+            ck.set_ptr = cptr_.data();
+            ck.items = oi.data();
+            ck.support = csup_.data();
+            ck.nodes = nodes_;
+            if (cb(user, &ck) != 0) break;
+        }
+    }
+    int rc = finish(out);
+    h_->launches += launches_;
+    return rc;
+}
+
+int Miner::finish(sgfim_result **out) {
+    const uint64_t n = csup_.size();
+    // maximality filter: members of the pool containing each candidate
+    std::vector<uint32_t> keep(n, 1);
+    if (n > 1) {
+        const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
+        const uint64_t chunk = 1u << 20;
+        QuerySet qs;
+        std::vector<uint32_t> cnt;
+        for (uint64_t a = 0; a < n; a += chunk) {
+            const uint64_t b = std::min(n, a + chunk);
+            qs.clear();
+            for (uint64_t c = a; c < b; ++c) qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
+            run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_COUNT, cnt);
+            for (uint64_t c = a; c < b; ++c) keep[c] = cnt[c - a] <= 1;
+        }
+    }
+    // root rule: the highest original id of the set must be a root
+    std::vector<uint8_t> is_root;
+    if (p_.root_rule == SGFIM_ROOTS_LIST) {
+        is_root.assign(ds_.d, 0);
+        for (uint32_t i = 0; i < p_.n_roots; ++i) {
+            const uint32_t id = p_.roots[i];
+            if (id < ds_.n_ids && ds_.o2d[id] >= 0) is_root[ds_.o2d[id]] = 1;
+        }
+    } else if (p_.root_rule == SGFIM_ROOTS_MINCOUNT) {
+        is_root.assign(ds_.d, 0);
+        for (uint32_t e = 0; e < ds_.d; ++e) is_root[e] = ds_.occ[ds_.d2o[e]] >= p_.root_min_count;
+    }
+    std::vector<uint64_t> order;
+    for (uint64_t c = 0; c < n; ++c) {
+        if (!keep[c]) continue;
+        if (!is_root.empty()) {
+            const uint32_t top = citems_[cptr_[c + 1] - 1];  // dense ids ascend with original ids
+            if (!is_root[top]) continue;
+        }
+        order.push_back(c);
+    }
+    // deterministic order: support descending, then items lexicographic
+    std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+        if (csup_[a] != csup_[b]) return csup_[a] > csup_[b];
+        return std::lexicographical_compare(citems_.begin() + cptr_[a], citems_.begin() + cptr_[a + 1],
+                                            citems_.begin() + cptr_[b], citems_.begin() + cptr_[b + 1]);
+    });
+    sgfim_result *r = static_cast<sgfim_result *>(calloc(1, sizeof(sgfim_result)));
+    if (!r) return fail(h_, SGFIM_ENOMEM, "result allocation failed");
+    const uint64_t m = order.size();
+    uint64_t total = 0;
+    for (uint64_t c : order) total += cptr_[c + 1] - cptr_[c];
+    r->n_sets = m;
+    r->set_ptr = static_cast<uint64_t *>(malloc((m + 1) * 8));
+    r->items = static_cast<uint32_t *>(malloc(std::max<uint64_t>(total, 1) * 4));
+    r->support = static_cast<uint32_t *>(malloc(std::max<uint64_t>(m, 1) * 4));
+    r->emit_time_s = static_cast<double *>(malloc(std::max<uint64_t>(m, 1) * 8));
+    if (!r->set_ptr || !r->items || !r->support || !r->emit_time_s) {
+        sgfim_result_free(r);
+        return fail(h_, SGFIM_ENOMEM, "result allocation failed");
+    }
+    r->set_ptr[0] = 0;
+    uint64_t pos = 0;
+    for (uint64_t i = 0; i < m; ++i) {
+        const uint64_t c = order[i];
+        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[pos++] = ds_.d2o[citems_[k]];
+        r->set_ptr[i + 1] = pos;
+        r->support[i] = csup_[c];
+        r->emit_time_s[i] = ctime_[c];
+    }
+    r->n_txn = ds_.n_txn;
+    r->min_count = thr_;
+    r->elapsed_s = elapsed();
+    r->nodes = nodes_;
+    r->waves = waves_;
+    r->kernel_launches = launches_;
+    r->candidates = n;
+    *out = r;
+    return SGFIM_OK;
+}
+
+}  // namespace
+
+int mine_impl(sgfim_handle *h, const sgfim_mine_params *p, const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb,
+              void *user, sgfim_result **out) {
+    *out = nullptr;
+    if (p->root_rule > SGFIM_ROOTS_MINCOUNT) return fail(h, SGFIM_EINVAL, "unknown root rule");
+    if (p->root_rule == SGFIM_ROOTS_LIST && p->n_roots && !p->roots) return fail(h, SGFIM_EINVAL, "null roots");
+    if (!h->ds.loaded) return fail(h, SGFIM_ESTATE, "no dataset loaded");
+    if (h->ds.n_txn == 0 || h->ds.d == 0) {
+        // nothing to mine: an empty, valid result
+        Miner m(h, *p);
+        sgfim_mine_params q = *p;
+        (void)q;
+        sgfim_result *r = static_cast<sgfim_result *>(calloc(1, sizeof(sgfim_result)));
+        if (!r) return fail(h, SGFIM_ENOMEM, "result allocation failed");
+        r->set_ptr = static_cast<uint64_t *>(calloc(1, 8));
+        r->items = static_cast<uint32_t *>(calloc(1, 4));
+        r->support = static_cast<uint32_t *>(calloc(1, 4));
+        r->emit_time_s = static_cast<double *>(calloc(1, 8));
+        r->n_txn = h->ds.n_txn;
+        r->min_count = p->min_count;
+        *out = r;
+        return SGFIM_OK;
+    }
+    Miner m(h, *p);
+    int rc = m.run(ckpts, n_ckpt, cb, user, out);
+    if (rc != SGFIM_OK) return rc;
+    return check_device_error(h);
+}
+
+}  // namespace sg

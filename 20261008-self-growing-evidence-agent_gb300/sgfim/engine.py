@@ -1,0 +1,257 @@
+"""Python front end of the sgfim engine (a thin layer over the C ABI).
+
+``Engine`` keeps one handle: bitmaps stay resident on the GPU between calls.
+Methods map one-to-one onto include/sgfim.h; item ids are original ids.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = ["Engine", "SgfimError", "MineResult"]
+
+
+class SgfimError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sgfim error {code}: {msg}")
+        self.code = code
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class MineResult:
+    """MFIs as (tuple of original ids ascending, support), plus run statistics."""
+
+    def __init__(self, res_ptr):
+        r = res_ptr.contents
+        n = int(r.n_sets)
+        ptr = np.ctypeslib.as_array(r.set_ptr, shape=(n + 1,)).copy() if n else np.zeros(1, np.uint64)
+        tot = int(ptr[-1])
+        self.items = np.ctypeslib.as_array(r.items, shape=(tot,)).copy() if tot else np.zeros(0, np.uint32)
+        self.support = np.ctypeslib.as_array(r.support, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        self.emit_time_s = np.ctypeslib.as_array(r.emit_time_s, shape=(n,)).copy() if n else np.zeros(0)
+        self.ptr = ptr
+        self.n_txn = int(r.n_txn)
+        self.min_count = int(r.min_count)
+        self.elapsed_s = float(r.elapsed_s)
+        self.nodes = int(r.nodes)
+        self.waves = int(r.waves)
+        self.kernel_launches = int(r.kernel_launches)
+        self.candidates = int(r.candidates)
+
+    def __len__(self):
+        return len(self.support)
+
+    def sets(self):
+        p, it = self.ptr, self.items
+        return [(tuple(int(x) for x in it[p[i]:p[i + 1]]), int(self.support[i])) for i in range(len(self))]
+
+    def as_dict(self):
+        return {frozenset(s): c for s, c in self.sets()}
+
+
+class Engine:
+    def __init__(self, device=0, hbm_budget=0, wave_nodes=0, verbose=False, phase_timers=False,
+                 ignore_id0=False):
+        self._L = L.load()
+        flags = (L.F_VERBOSE if verbose else 0) | (L.F_PHASE_TIMERS if phase_timers else 0) | \
+            (L.F_IGNORE_ID0 if ignore_id0 else 0)
+        cfg = L.Config(device, hbm_budget, wave_nodes, flags, None)
+        h = C.c_void_p()
+        rc = self._L.sgfim_open(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise SgfimError(rc, "sgfim_open failed (no CUDA device?)")
+        self._h = h
+        self._keep = []
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, rc):
+        if rc != 0:
+            msg = self._L.sgfim_last_error(self._h)
+            raise SgfimError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sgfim_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ------------------------------------------------------------ loading
+    def load_fimi(self, path):
+        self._check(self._L.sgfim_load_fimi(self._h, os.fsencode(path)))
+        return self
+
+    def load_csr(self, row_ptr, items):
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.uint64)
+        items = np.ascontiguousarray(items, dtype=np.uint32)
+        if len(items) == 0:
+            items = np.zeros(1, np.uint32)
+        self._check(self._L.sgfim_load_csr(self._h, _p(row_ptr, C.c_uint64), _p(items, C.c_uint32),
+                                           len(row_ptr) - 1))
+        return self
+
+    def load_rows(self, rows):
+        from .datagen import txns_to_csr
+        return self.load_csr(*txns_to_csr(rows))
+
+    def load_bitmaps(self, bm, n_txn):
+        bm = np.ascontiguousarray(bm, dtype=np.uint64)
+        d, w = bm.shape
+        self._check(self._L.sgfim_load_bitmaps(self._h, _p(bm, C.c_uint64), d, int(n_txn), w))
+        return self
+
+    def info(self):
+        i = L.DatasetInfo()
+        self._check(self._L.sgfim_dataset_info_get(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in L.DatasetInfo._fields_}
+
+    def item_counts(self, n=None):
+        if n is None:
+            n = self.info()["n_ids"]
+        out = np.zeros(max(n, 1), dtype=np.uint32)
+        self._check(self._L.sgfim_item_counts(self._h, _p(out, C.c_uint32), n))
+        return out[:n]
+
+    # ------------------------------------------------------------ counting
+    def support_batch(self, cand_ptr, cand_items):
+        cand_ptr = np.ascontiguousarray(cand_ptr, dtype=np.uint64)
+        cand_items = np.ascontiguousarray(cand_items, dtype=np.uint32)
+        if len(cand_items) == 0:
+            cand_items = np.zeros(1, np.uint32)
+        n = len(cand_ptr) - 1
+        out = np.zeros(max(n, 1), dtype=np.uint32)
+        self._check(self._L.sgfim_support_batch(self._h, _p(cand_ptr, C.c_uint64), _p(cand_items, C.c_uint32),
+                                                n, _p(out, C.c_uint32)))
+        return out[:n]
+
+    def support_batch_device(self, bm_ptr, d, n_words, row_stride, cand_ptr_ptr, cand_items_ptr, n_cand,
+                             out_ptr, stream=0):
+        self._check(self._L.sgfim_support_batch_device(self._h, bm_ptr, d, n_words, row_stride, cand_ptr_ptr,
+                                                       cand_items_ptr, n_cand, out_ptr, stream or None))
+
+    def phase_stats(self, reset=True):
+        """Summed CUDA-event phase times of support-batch calls (needs phase_timers=True)."""
+        s = L.PhaseStats()
+        self._check(self._L.sgfim_phase_stats_get(self._h, C.byref(s), 1 if reset else 0))
+        return {k: getattr(s, k) for k, _ in L.PhaseStats._fields_}
+
+    def cooccurrence(self):
+        """d x d co-occurrence of the bitmap rows (d = info()['rows'])."""
+        d = self.info()["rows"]
+        out = np.zeros((max(d, 1), max(d, 1)), dtype=np.uint32)
+        self._check(self._L.sgfim_cooccurrence(self._h, _p(out, C.c_uint32), d))
+        return out[:d, :d]
+
+    def cooccurrence_device(self, bm_ptr, d, n_words, row_stride, out_ptr, kind=L.COOC_AUTO, stream=0):
+        self._check(self._L.sgfim_cooccurrence_device(self._h, bm_ptr, d, n_words, row_stride, out_ptr, kind,
+                                                      stream or None))
+
+    # ------------------------------------------------------------ mining
+    def _params(self, min_count, roots=None, root_min_count=None, order="support", time_limit_s=0.0,
+                node_limit=0):
+        p = L.MineParams()
+        p.min_count = int(min_count)
+        p.root_rule = L.ROOTS_ALL
+        if roots is not None:
+            r = np.ascontiguousarray(roots, dtype=np.uint32)
+            if len(r) == 0:
+                r = np.zeros(1, np.uint32)
+                p.n_roots = 0
+            else:
+                p.n_roots = len(r)
+            self._keep.append(r)
+            p.roots = _p(r, C.c_uint32)
+            p.root_rule = L.ROOTS_LIST
+        elif root_min_count is not None:
+            p.root_rule = L.ROOTS_MINCOUNT
+            p.root_min_count = int(root_min_count)
+        p.order = L.ORDER_LEARNED if order == "learned" else L.ORDER_SUPPORT
+        p.time_limit_s = float(time_limit_s)
+        p.node_limit = int(node_limit)
+        return p
+
+    def mine(self, min_count, **kw):
+        """Exact MFIs at absolute threshold ``min_count`` (see sgfim_mine)."""
+        p = self._params(min_count, **kw)
+        res = C.POINTER(L.Result)()
+        rc = self._L.sgfim_mine(self._h, C.byref(p), C.byref(res))
+        self._keep.clear()
+        self._check(rc)
+        try:
+            return MineResult(res)
+        finally:
+            self._L.sgfim_result_free(res)
+
+    def mine_anytime(self, min_count, checkpoints, callback=None, **kw):
+        """Mine with wall-clock checkpoints.  ``callback(t_s, elapsed_s, sets)``
+        receives the emitted candidates as a list of (ids tuple, support);
+        returning True stops the search.  Returns (result, records)."""
+        p = self._params(min_count, **kw)
+        cks = np.ascontiguousarray(checkpoints, dtype=np.float64)
+        records = []
+
+        def _cb(user, ckp):
+            ck = ckp.contents
+            n = int(ck.n_emitted)
+            ptr = np.ctypeslib.as_array(ck.set_ptr, shape=(n + 1,)) if n else np.zeros(1, np.uint64)
+            tot = int(ptr[-1])
+            it = np.ctypeslib.as_array(ck.items, shape=(tot,)) if tot else np.zeros(0, np.uint32)
+            sp = np.ctypeslib.as_array(ck.support, shape=(n,)) if n else np.zeros(0, np.uint32)
+            sets = [(tuple(int(x) for x in it[ptr[i]:ptr[i + 1]]), int(sp[i])) for i in range(n)]
+            records.append({"t_s": ck.t_s, "elapsed_s": ck.elapsed_s, "n_emitted": n, "nodes": int(ck.nodes),
+                            "sets": sets})
+            if callback is not None:
+                return 1 if callback(ck.t_s, ck.elapsed_s, sets) else 0
+            return 0
+
+        cb = L.CKPT_CB(_cb)
+        res = C.POINTER(L.Result)()
+        rc = self._L.sgfim_mine_anytime(self._h, C.byref(p), _p(cks, C.c_double) if len(cks) else None,
+                                        len(cks), cb, None, C.byref(res))
+        self._keep.clear()
+        self._check(rc)
+        try:
+            return MineResult(res), records
+        finally:
+            self._L.sgfim_result_free(res)
+
+    # ------------------------------------------------------------ scoring
+    def load_scorer(self, w1, b1, w2, b2, w3, b3):
+        """Weights as float arrays (converted to bf16 here, round-to-nearest-even)."""
+        from .mlp import to_bf16_bits
+        ws = [np.ascontiguousarray(to_bf16_bits(w)) for w in (w1, w2, w3)]
+        bs = [np.ascontiguousarray(b, dtype=np.float32) for b in (b1, b2, b3)]
+        hidden, in_dim = w1.shape
+        self._check(self._L.sgfim_load_scorer(self._h, in_dim, hidden,
+                                              _p(ws[0], C.c_uint16), _p(bs[0], C.c_float),
+                                              _p(ws[1], C.c_uint16), _p(bs[1], C.c_float),
+                                              _p(ws[2], C.c_uint16), _p(bs[2], C.c_float)))
+
+
+def thresh_from(n, min_sup=0.05, min_count=None):
+    """The reference's threshold rule (code/pipeline/skab_spike.py:99-100)."""
+    if min_count is not None:
+        return max(1, int(min_count))
+    return max(1, int(math.ceil(float(np.float64(min_sup) * n))))

@@ -1,0 +1,263 @@
+/*
+ * sgfim.h -- C ABI of the GB300 maximal-frequent-itemset (MFI) engine.
+ *
+ * The reference drives its engines as executables
+ * (code/pipeline/engine_adapter.py:70-100 runs `CoParaCG_{baseline,bmma}.exe
+ * <fimi> <rel_thr>`, :115-131 runs `AnytimeMining.exe <fimi> <upto_stage>`)
+ * and reads their `*=Results.txt` files back.  This library offers the same
+ * path as plain C calls: a caller binds it with ctypes (or cgo/JNI/N-API)
+ * and never sees a CUDA or PyTorch type.  The CLI shims built on top of it
+ * write byte-compatible Results.txt files, so engine_adapter.py keeps working.
+ *
+ * Conventions
+ *   - Return codes: SGFIM_OK (0) or a negative SGFIM_E* code; no call exits
+ *     the process.  sgfim_last_error() gives the message of the last failure
+ *     on a handle.
+ *   - Item ids at the ABI are ORIGINAL ids (the integers of the FIMI file or
+ *     the rows of a bitmap matrix).  Internally items are remapped to dense
+ *     ids in ascending original-id order.
+ *   - Results are allocated by the engine and released with
+ *     sgfim_result_free().  Itemsets come back as CSR arrays of original ids,
+ *     ascending inside each set, with uint32 supports (absolute counts).
+ *   - One handle per host thread; a handle is not reentrant.  Callbacks run
+ *     on the calling thread.
+ *   - Every device wait inside the engine's kernels is bounded; a wait that
+ *     runs out makes the call return SGFIM_EDEVICE without hanging the GPU.
+ */
+#ifndef SGFIM_H
+#define SGFIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGFIM_ABI_VERSION 1
+
+enum {
+    SGFIM_OK = 0,
+    SGFIM_EINVAL = -1,     /* bad argument */
+    SGFIM_ENOMEM = -2,     /* host or device allocation failed / budget exceeded */
+    SGFIM_EIO = -3,        /* file could not be read or written */
+    SGFIM_EDEVICE = -4,    /* CUDA error or bounded device wait ran out */
+    SGFIM_ESTATE = -5,     /* call out of order (e.g. mining before loading) */
+    SGFIM_ETIMEDOUT = -6,  /* the caller's time limit expired */
+    SGFIM_ECANCELED = -7,  /* a checkpoint callback asked to stop */
+    SGFIM_ENODATA = -8     /* no transactions loaded */
+};
+
+typedef struct sgfim_handle sgfim_handle;
+
+typedef struct {
+    int device;               /* CUDA device ordinal */
+    uint64_t hbm_budget;      /* bytes of device memory the engine may use; 0 = 90% of free */
+    uint32_t wave_nodes;      /* search nodes expanded per wave; 0 = engine default */
+    uint32_t flags;           /* SGFIM_F_* */
+    const char *tune_cache;   /* autotuner cache file (JSON); NULL = none */
+} sgfim_config;
+
+#define SGFIM_F_VERBOSE 0x1u   /* print phase timers to stderr */
+#define SGFIM_F_IGNORE_ID0 0x2u /* loads drop item id 0: the TensorFIM and AnyFIM engines never
+                                   use id 0 as a candidate (kernel_bitmap.cu:354-356,
+                                   AnytimeMining/kernel.cu:338-341) */
+#define SGFIM_F_PHASE_TIMERS 0x4u /* record per-kernel CUDA events in support-batch calls */
+
+/* Open a handle on a device.  Replaces the engines' process start-up
+ * (kernel_bitmap.cu:796-800, AnytimeMining/kernel.cu:798-805). */
+int sgfim_open(const sgfim_config *cfg, sgfim_handle **out);
+void sgfim_close(sgfim_handle *h);
+const char *sgfim_last_error(const sgfim_handle *h);
+int sgfim_abi_version(void);
+
+/* ---------------------------------------------------------------- loading */
+
+/* Parse a FIMI file: one transaction per '\n', whitespace-separated
+ * non-negative integers; a '-' and the digits after it are dropped; a final
+ * line without '\n' counts when it holds an item.  Replaces readTransSetFile
+ * (code/engine_tensorfim/code/engine/src/kernel_bitmap.cu:205-267). */
+int sgfim_load_fimi(sgfim_handle *h, const char *path);
+
+/* Load transactions from CSR host arrays of original ids:
+ * transaction t holds items[row_ptr[t] .. row_ptr[t+1]).  Duplicate ids in
+ * a row count once in the bitmap (the bitmap ORs bits, kernel_bitmap.cu:374-379). */
+int sgfim_load_csr(sgfim_handle *h, const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn);
+
+/* Load vertical bitmaps directly (host memory): row e (original id e,
+ * 0 <= e < d) holds n_words uint64 words; bit t&63 of word t>>6 is
+ * transaction t; bits at t >= n_txn must be zero. */
+int sgfim_load_bitmaps(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uint64_t n_txn,
+                       uint64_t n_words);
+
+typedef struct {
+    uint64_t n_txn;          /* transNum */
+    uint32_t n_ids;          /* itemIDmax + 1 */
+    uint32_t n_present;      /* distinct ids that occur (the reference's "dimension") */
+    uint32_t id_min, id_max; /* itemIDmin / itemIDmax over present ids */
+    uint64_t len_min, len_max; /* transaction length extremes */
+    double len_mean;
+    uint64_t words;          /* uint64 words per item bitmap row (padded) */
+    uint32_t rows;           /* bitmap rows: present ids in ascending order (FIMI/CSR
+                                loads) or every row (bitmap loads) */
+} sgfim_dataset_info;
+
+int sgfim_dataset_info_get(sgfim_handle *h, sgfim_dataset_info *out);
+
+/* Singleton supports of ids 0..n-1 (getItemsFrequenc, kernel_bitmap.cu:269-275). */
+int sgfim_item_counts(sgfim_handle *h, uint32_t *out, uint32_t n);
+
+/* ---------------------------------------------------------------- counting */
+
+/* Supports of n_cand itemsets given as CSR over original ids:
+ * out[c] = |{t : items[cand_ptr[c]..cand_ptr[c+1]) all in t}|.
+ * The batched form of getResFrequencyCuda (kernel_bitmap.cu:412-536) and of
+ * the wave engine's batchCountBMMA (kernel_bmma.cu:772-872).  An empty
+ * itemset has support n_txn; an id that never occurs gives 0. */
+int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_t *cand_items,
+                        uint64_t n_cand, uint32_t *out);
+
+/* Device-pointer form for callers whose data already sits in HBM.
+ * bitmaps: d rows of row_stride uint64 words (row_stride even, base 16-byte
+ * aligned), n_words valid words per row; cand_ptr/cand_items: CSR in device
+ * memory (items are row indices); out: n_cand uint32 in device memory.
+ * stream: a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Asynchronous: returns after enqueueing the work. */
+int sgfim_support_batch_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
+                               uint64_t row_stride, const uint64_t *cand_ptr, const uint32_t *cand_items,
+                               uint64_t n_cand, uint32_t *out, void *stream);
+
+/* Pairwise co-occurrence C[i][j] = |{t : i in t and j in t}| of the loaded
+ * bitmap rows (d x d uint32, row-major, host memory; d = info.rows, row i is
+ * the i-th present id in ascending order for FIMI/CSR loads).  The reference's
+ * equivalent is the b1 AND-POPC GEMM of bmma_bench.cu:99-152 with A = B =
+ * the item bitmaps. */
+int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
+
+/* Phase timers (CUDA events on the launching stream) of the batched support
+ * path, enabled by SGFIM_F_PHASE_TIMERS; the counterpart of the wave engine's
+ * g_tMask / g_tBmma / g_tCopy timers (kernel_bmma.cu:385,817-869).
+ * sgfim_phase_stats_get waits for the recorded events, sums them over every
+ * call since the last reset and optionally resets. */
+typedef struct {
+    uint64_t calls;          /* timed support-batch calls */
+    uint64_t launches;       /* kernels launched by those calls */
+    double prep_ms;          /* candidate packing */
+    double count_ms;         /* the staged (or streaming) counting kernel */
+    double tail_ms;          /* candidates with more than 8 items */
+} sgfim_phase_stats;
+int sgfim_phase_stats_get(sgfim_handle *h, sgfim_phase_stats *out, int reset);
+
+/* Device-pointer form: bitmaps as in sgfim_support_batch_device, out d*d
+ * uint32 in device memory.  kind: SGFIM_COOC_* (AUTO picks the tuned one). */
+#define SGFIM_COOC_AUTO 0
+#define SGFIM_COOC_POPC 1     /* CUDA-core AND + popc, register tiled */
+#define SGFIM_COOC_BMMA 2     /* b1 mma.sync AND-POPC on the tensor pipe */
+#define SGFIM_COOC_TC_F8 3    /* tcgen05 e4m3 GEMM of 0/1 bytes, fp32 accumulate */
+int sgfim_cooccurrence_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
+                              uint64_t row_stride, uint32_t *out, int kind, void *stream);
+
+/* ---------------------------------------------------------------- mining */
+
+typedef struct {
+    uint64_t n_sets;
+    uint64_t *set_ptr;       /* n_sets + 1 offsets into items */
+    uint32_t *items;         /* original ids, ascending inside a set */
+    uint32_t *support;       /* absolute supports */
+    double *emit_time_s;     /* seconds from the start of the call when each set was emitted */
+    uint64_t n_txn;          /* transactions in the loaded database */
+    uint32_t min_count;      /* absolute threshold used */
+    double elapsed_s;        /* wall time of the mining call */
+    double preprocess_s;     /* part of elapsed_s spent building bitmaps */
+    uint64_t nodes;          /* search nodes expanded */
+    uint64_t waves;          /* device waves */
+    uint64_t kernel_launches;
+    uint64_t candidates;     /* candidate MFIs emitted before the final maximality filter */
+} sgfim_result;
+
+/* Root rules: which items may be the highest-id item of a reported MFI. */
+#define SGFIM_ROOTS_ALL 0     /* every frequent item: the complete MFI set (mine_mfi, skab_spike.py:84-135) */
+#define SGFIM_ROOTS_LIST 1    /* the ids in `roots` (AnyFIM stage k: the top-k ids, AnytimeMining/kernel.cu:850-859) */
+#define SGFIM_ROOTS_MINCOUNT 2 /* ids with count >= root_min_count (TensorFIM: count/n > thr, kernel_bmma.cu:1199,1224-1233) */
+
+/* Frontier orders (change the order of emission, never the result). */
+#define SGFIM_ORDER_SUPPORT 0 /* canonical: tail items by ascending support */
+#define SGFIM_ORDER_LEARNED 1 /* priority from the loaded scoring MLP */
+
+typedef struct {
+    uint32_t min_count;       /* absolute support threshold (>= 1) */
+    uint32_t root_rule;       /* SGFIM_ROOTS_* */
+    const uint32_t *roots;    /* SGFIM_ROOTS_LIST: original ids */
+    uint32_t n_roots;
+    uint32_t root_min_count;  /* SGFIM_ROOTS_MINCOUNT */
+    uint32_t order;           /* SGFIM_ORDER_* */
+    double time_limit_s;      /* 0 = none; expiry returns SGFIM_ETIMEDOUT */
+    uint64_t node_limit;      /* 0 = none; exceeding it returns SGFIM_ENOMEM */
+} sgfim_mine_params;
+
+/* Exact MFI set {M in MFI(min_count) : max(M) in roots}.  With
+ * SGFIM_ROOTS_ALL this equals mine_mfi(txns, min_count=...) of
+ * code/pipeline/skab_spike.py:84-135 as a set of (itemset, support). */
+int sgfim_mine(sgfim_handle *h, const sgfim_mine_params *p, sgfim_result **out);
+
+/* Anytime mining at a support floor with wall-clock checkpoints.  The
+ * callback runs at each checkpoint (seconds from the call's start) with the
+ * candidate MFIs emitted so far; returning non-zero stops the search
+ * (SGFIM_ECANCELED).  The final result is exact; checkpoint pools hold every
+ * emitted candidate, which the final maximality filter may still drop. */
+typedef struct {
+    double t_s;               /* checkpoint time requested */
+    double elapsed_s;         /* actual time of the callback */
+    uint64_t n_emitted;       /* candidates emitted so far */
+    const uint64_t *set_ptr;  /* CSR of the emitted candidates (valid during the callback) */
+    const uint32_t *items;
+    const uint32_t *support;
+    uint64_t nodes;
+} sgfim_checkpoint;
+typedef int (*sgfim_ckpt_cb)(void *user, const sgfim_checkpoint *ck);
+
+int sgfim_mine_anytime(sgfim_handle *h, const sgfim_mine_params *p, const double *checkpoints_s,
+                       uint32_t n_checkpoints, sgfim_ckpt_cb cb, void *user, sgfim_result **out);
+
+void sgfim_result_free(sgfim_result *r);
+
+/* ---------------------------------------------------------------- output */
+
+/* Results.txt writers.  TENSORFIM: header + "List of MFIs" records sorted by
+ * frequency descending (kernel_bitmap.cu:651-690), parsed by
+ * engine_adapter.parse_tensorfim_results (engine_adapter.py:103-111). */
+typedef struct {
+    const char *trans_set_file;   /* echoed as transSetFile */
+    double support_threshold;     /* relative threshold echoed in the header */
+    double computation_time_s;
+    double preprocessing_time_s;
+    uint32_t dimension_reduced;
+} sgfim_tf_meta;
+int sgfim_write_tensorfim(sgfim_handle *h, const sgfim_result *r, const sgfim_tf_meta *meta, const char *path);
+
+/* ANYFIM: per-stage sections "==== <k>th stage MFIs Number: <m> ====" and the
+ * header arrays of AnytimeMining/kernel.cu:615-659, parsed by
+ * engine_adapter.parse_anyfim_results (engine_adapter.py:134-166). */
+typedef struct {
+    const char *trans_set_file;
+    uint32_t upto_stage;
+    double preprocessing_time_s;
+    const double *runtime_per_stage_s;    /* upto_stage values */
+    const uint32_t *frequency_thr_per_stage; /* upto_stage values */
+} sgfim_af_meta;
+int sgfim_write_anyfim(sgfim_handle *h, sgfim_result *const *stages, const sgfim_af_meta *meta,
+                       const char *path);
+
+/* ---------------------------------------------------------------- scoring */
+
+/* Load the frontier-scoring MLP used by SGFIM_ORDER_LEARNED: 3 layers,
+ * in_dim -> hidden -> hidden -> 1, bf16 weights (row-major [out][in]) and
+ * fp32 biases, ReLU between layers, sigmoid output. */
+int sgfim_load_scorer(sgfim_handle *h, uint32_t in_dim, uint32_t hidden, const uint16_t *w1_bf16,
+                      const float *b1, const uint16_t *w2_bf16, const float *b2, const uint16_t *w3_bf16,
+                      const float *b3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGFIM_H */

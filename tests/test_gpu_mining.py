@@ -1,0 +1,153 @@
+"""GPU miner parity: exact MFI sets and supports against the reference's own
+outputs (golden fixtures) and against the CPU oracle at larger sizes."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from sgfim import datagen, engine_adapter
+from sgfim.engine import thresh_from
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "mfi_golden.json")))["cases"]
+
+
+def rows_of(case):
+    g = case["gen"]
+    if g["kind"] == "regime":
+        r = datagen.regime_txns(g["n"], g["sensors"], g["bins"], g["regimes"], g["alpha"], seed=g["seed"])
+        return [list(map(int, x)) for x in r]
+    return [list(x) for x in g["rows"]]
+
+
+def canon_dict(d):
+    return sorted(([sorted(s), c] for s, c in d.items()), key=lambda t: (t[0], t[1]))
+
+
+@pytest.mark.parametrize("case", GOLD, ids=[c["name"] for c in GOLD])
+def test_mine_matches_reference_golden(engine, case):
+    rows = rows_of(case)
+    engine.load_csr(*datagen.txns_to_csr(rows))
+    kw = {"min_count": case["min_count"]} if "min_count" in case else {"min_sup": case["min_sup"]}
+    res = engine.mine(thresh_from(len(rows), **kw))
+    assert canon_dict(res.as_dict()) == case["mfis"]
+
+
+@pytest.mark.parametrize("n,sensors,bins,regimes,alpha,frac,seed", [
+    (100_000, 20, 8, 32, 0.2, 0.01, 0),     # anytime-2m shape, 20 sensors, 1% floor
+    (50_000, 80, 8, 32, 0.2, 0.08, 1),      # the full 640-item anytime-2m shape, 8% floor
+    (20_000, 21, 6, 8, 0.3, 0.03, 2),       # window shape
+])
+def test_mine_matches_oracle_larger(engine, n, sensors, bins, regimes, alpha, frac, seed):
+    rows = datagen.regime_txns(n, sensors, bins, regimes, alpha, seed=seed)
+    rp, it = datagen.txns_to_csr(rows)
+    engine.load_csr(rp, it)
+    thr = int(np.ceil(frac * n))
+    got = engine.mine(thr).as_dict()
+    bm, _ = oracle.build_bitmaps(rp, it, sensors * bins)
+    ref, _ = oracle.mine_fast(bm, n, thr)
+    assert got == {frozenset(s): c for s, c in ref}
+
+
+def test_mine_result_properties(engine):
+    """Size-independent checks on a 400,000-transaction, 640-item run: every
+    reported set is frequent with the exact support, none contains another, and
+    no single-item extension of a sample is frequent."""
+    n = 400_000
+    rows = datagen.regime_txns(n, 80, 8, 32, 0.2, seed=5)
+    rp, it = datagen.txns_to_csr(rows)
+    engine.load_csr(rp, it)
+    thr = int(0.06 * n)
+    res = engine.mine(thr)
+    sets = res.sets()
+    assert len(sets) > 100
+    cp = np.zeros(len(sets) + 1, np.uint64)
+    cp[1:] = np.cumsum([len(s) for s, _ in sets])
+    ci = np.array([x for s, _ in sets for x in s], np.uint32)
+    assert np.array_equal(engine.support_batch(cp, ci), np.array([c for _, c in sets], np.uint32))
+    fs = [frozenset(s) for s, _ in sets]
+    by_item = {}
+    for i, s in enumerate(fs):
+        for x in s:
+            by_item.setdefault(x, set()).add(i)
+    for i, s in enumerate(fs):
+        sup = set.intersection(*(by_item[x] for x in s))
+        assert sup == {i}, "a reported set is contained in another"
+    rng = np.random.default_rng(0)
+    sample = rng.choice(len(sets), min(200, len(sets)), replace=False)
+    ext_ptr, ext_items = [0], []
+    for i in sample:
+        s = list(sets[i][0])
+        for e in range(640):
+            if e not in s:
+                ext_items.extend(s + [e])
+                ext_ptr.append(len(ext_items))
+    ext = engine.support_batch(np.array(ext_ptr, np.uint64), np.array(ext_items, np.uint32))
+    assert (ext < thr).all()
+
+
+def test_root_rules_match_engine_semantics(engine):
+    rows = datagen.regime_txns(3000, 6, 5, 3, 0.4, seed=3)
+    rows1 = [[x + 1 for x in r] for r in rows.tolist()]
+    engine.load_csr(*datagen.txns_to_csr(rows1))
+    cnt = oracle.item_counts(rows1)
+    order = oracle.freq_order(cnt)
+    for k in (1, 4, 9, 17, 25):
+        thr = int(cnt[order[k - 1]])
+        got = engine.mine(thr, roots=[int(x) for x in order[:k]]).as_dict()
+        want = oracle.anyfim_stages(rows1, k)[k]
+        assert got == want, k
+    for rel in (0.05, 0.1, 0.2):
+        thr = max(1, int(np.ceil(len(rows1) * rel)))
+        root_min = int(np.floor(len(rows1) * rel))
+        while root_min / len(rows1) <= rel:
+            root_min += 1
+        got = engine.mine(thr, root_min_count=root_min).as_dict()
+        assert got == oracle.tensorfim_mfis(rows1, rel), rel
+
+
+def test_anytime_checkpoints(engine):
+    rows = datagen.regime_txns(60_000, 40, 8, 32, 0.2, seed=8)
+    rp, it = datagen.txns_to_csr(rows)
+    engine.load_csr(rp, it)
+    thr = int(0.02 * 60_000)
+    res, recs = engine.mine_anytime(thr, [0.0, 0.05, 0.2, 1e6])
+    final = res.as_dict()
+    assert len(recs) == 4
+    counts = [r["n_emitted"] for r in recs]
+    assert counts == sorted(counts)
+    emitted = {frozenset(s): c for s, c in recs[-1]["sets"]}
+    assert set(final) <= set(emitted)
+    assert all(emitted[s] == c for s, c in final.items())
+    assert res.emit_time_s.max() <= res.elapsed_s + 1e-6
+    bm, _ = oracle.build_bitmaps(rp, it, 320)
+    ref, _ = oracle.mine_fast(bm, 60_000, thr)
+    assert final == {frozenset(s): c for s, c in ref}
+
+
+def test_cancel_from_checkpoint(engine):
+    from sgfim.engine import SgfimError
+    rows = datagen.regime_txns(30_000, 30, 8, 32, 0.2, seed=9)
+    engine.load_rows(rows)
+    with pytest.raises(SgfimError) as ei:
+        engine.mine_anytime(int(0.02 * 30_000), [0.0], callback=lambda t, e, s: True)
+    assert ei.value.code == -7
+
+
+def test_cli_shims_through_adapter(tmp_path):
+    rows = datagen.regime_txns(4000, 8, 5, 4, 0.3, seed=12)
+    rows1 = [[x + 1 for x in r] for r in rows.tolist()]
+    fimi = str(tmp_path / "d.txt")
+    datagen.write_fimi_ids(fimi, rows, one_based=True)
+    r = engine_adapter.run_tensorfim("bmma", fimi, 0.03)
+    assert r["ok"] and r["comp_times"] and r["tot_times"]
+    assert r["mfis"] == oracle.tensorfim_mfis(rows1, 0.03)
+    a = engine_adapter.run_anyfim(fimi, 12)
+    assert a["ok"]
+    want = oracle.anyfim_stages(rows1, 12)
+    assert {k: dict(v) for k, v in a["stages"].items()} == want
+    assert len(a["meta"]["runtimePerStage(s)"]) == 12
+    assert a["meta"]["MFIsNumPerStage"] == [len(want[k]) for k in range(1, 13)]

@@ -1,0 +1,164 @@
+"""Host-side tests that need no GPU: ABI exports, parsers, adapter mirror,
+workload generators, and the multi-process sharding of the bench path."""
+import json
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+from sgfim import datagen, engine_adapter
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "sgfim.h")
+ADAPTER_GOLD = json.load(open(os.path.join(ROOT, "tests", "golden", "adapter_golden.json")))
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sgfim_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from sgfim import _lib
+    L = _lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 19
+    for s in syms:
+        assert hasattr(L, s), f"libsgfim.so does not export {s}"
+    assert set(syms) <= set(_lib.SIGNATURES), "ctypes binding misses a declared symbol"
+    assert L.sgfim_abi_version() == 1
+
+
+def test_open_without_gpu_returns_error_code():
+    """With no CUDA device the ABI returns an error code instead of crashing."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from sgfim.engine import Engine, SgfimError
+    with pytest.raises(SgfimError):
+        Engine()
+
+
+def test_cli_usage_exit_code():
+    from sgfim import _lib
+    exe = os.path.join(os.path.dirname(_lib.LIB_PATH), "sgfim_tensorfim")
+    p = subprocess.run([exe], capture_output=True)
+    assert p.returncode == 2 and b"usage" in p.stderr
+
+
+# ------------------------------------------------------------------ FIMI parsing
+def test_parse_fimi_byte_rules(tmp_path):
+    p = tmp_path / "x.txt"
+    p.write_bytes(b"1 2 3\n\n4 -5 6\n7\t8,9\n  \n10 11")
+    rows = oracle.parse_fimi(str(p))
+    assert rows == [[1, 2, 3], [], [4, 6], [7, 8, 9], [], [10, 11]]
+    p.write_bytes(b"1 2\n3\n")
+    assert oracle.parse_fimi(str(p)) == [[1, 2], [3]]
+    p.write_bytes(b"1 2\n-3\n")
+    assert oracle.parse_fimi(str(p)) == [[1, 2], []]
+
+
+# ------------------------------------------------------------------ adapter mirror
+def test_adapter_regexes_equal_reference():
+    assert engine_adapter.TF_LINE.pattern == ADAPTER_GOLD["tf_line"]
+    assert engine_adapter.AF_STAGE.pattern == ADAPTER_GOLD["af_stage"]
+    assert engine_adapter.TF_COMP.pattern == ADAPTER_GOLD["tf_comp"]
+    assert engine_adapter.TF_TOT.pattern == ADAPTER_GOLD["tf_tot"]
+
+
+def test_adapter_parsers_match_reference_outputs(tmp_path):
+    p1, p2 = tmp_path / "tf.txt", tmp_path / "af.txt"
+    p1.write_text(ADAPTER_GOLD["tf_text"])
+    p2.write_text(ADAPTER_GOLD["af_text"])
+    tf = engine_adapter.parse_tensorfim_results(str(p1))
+    assert sorted([sorted(k), v] for k, v in tf.items()) == ADAPTER_GOLD["tf_parsed"]
+    st, meta = engine_adapter.parse_anyfim_results(str(p2))
+    assert {str(k): sorted([sorted(s), f] for s, f in v) for k, v in st.items()} == ADAPTER_GOLD["af_parsed"]
+    assert meta == ADAPTER_GOLD["af_meta"]
+    cum = engine_adapter.cumulative_mfis(st)
+    assert {str(k): sorted(sorted(s) for s in v) for k, v in cum.items()} == ADAPTER_GOLD["cumulative"]
+
+
+def test_write_fimi_numbering(tmp_path):
+    p = tmp_path / "t.txt"
+    m = engine_adapter.write_fimi([["a=1", "b=2"], ["b=2", "c=0", "b=2"], []], str(p), str(tmp_path / "m.json"))
+    assert m == {"a=1": 1, "b=2": 2, "c=0": 3}
+    assert p.read_text() == "1 2\n2 3\n\n"
+    inv = {v: k for k, v in engine_adapter.load_items_map(str(tmp_path / "m.json")).items()}
+    assert engine_adapter.decode_itemset([1, 3], inv) == frozenset({"a=1", "c=0"})
+
+
+def test_support_confidence_lift():
+    txns = [[1, 2], [1], [1, 2, 3], [2]]
+    sup, conf, lift = engine_adapter.support_confidence_lift({1, 2}, txns, [1, 0, 1, 0])
+    assert sup == 0.5 and conf == 1.0 and lift == 2.0
+
+
+# ------------------------------------------------------------------ generators
+def test_generators_shapes_and_determinism():
+    a = datagen.regime_txns(1000, 8, 5, 4, 0.3, seed=0)
+    b = datagen.regime_txns(1000, 8, 5, 4, 0.3, seed=0)
+    assert np.array_equal(a, b) and a.shape == (1000, 8)
+    assert (a // 5 == np.arange(8)[None, :]).all()  # one item per sensor
+    bm = datagen.correlated_bitmaps(4096, 32, 4, 0.02, 0.2, seed=1)
+    dens = np.unpackbits(bm.view(np.uint8), axis=1).mean(axis=1)
+    assert bm.shape == (32, 64) and (dens > 0.002).all() and (dens < 0.5).all()
+    cp, ci = datagen.walk_candidates(500, 64, 3, 8, seed=2)
+    k = np.diff(cp)
+    assert k.min() >= 3 and k.max() <= 8
+    for c in range(500):
+        s = ci[cp[c]:cp[c + 1]]
+        assert len(set(s.tolist())) == len(s) and (np.diff(s.astype(np.int64)) > 0).all()
+
+
+def test_csr_bitmap_roundtrip():
+    rows = datagen.regime_txns(777, 6, 4, 3, 0.3, seed=4)
+    rp, it = datagen.txns_to_csr(rows)
+    ref, _ = oracle.build_bitmaps(rp, it, 24)
+    assert np.array_equal(datagen.csr_to_bitmaps(rp, it, 24), ref)
+
+
+# ------------------------------------------------------------------ sharding (N>1 bench path)
+def _shard_worker(rank, world, port, result_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import torch
+    from sgfim.sharding import shard_range
+    bm = datagen.correlated_bitmaps(4096, 40, 4, 0.05, 0.3, seed=3)
+    cp, ci = datagen.walk_candidates(1001, 40, 3, 8, seed=4)
+    lo, hi = shard_range(len(cp) - 1, rank, world)
+    sub_ptr = cp[lo:hi + 1] - cp[lo]
+    sub_items = ci[cp[lo]:cp[hi]]
+    part = oracle.support_batch(bm, sub_ptr, sub_items, n_threads=1)
+    sizes = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(sizes, torch.tensor([len(part)]))
+    mx = int(max(s.item() for s in sizes))
+    buf = torch.zeros(mx, dtype=torch.int64)
+    buf[:len(part)] = torch.from_numpy(part.astype(np.int64))
+    outs = [torch.zeros(mx, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(outs, buf)
+    if rank == 0:
+        full = np.concatenate([o[:int(s.item())].numpy() for o, s in zip(outs, sizes)])
+        ref = oracle.support_batch(bm, cp, ci, n_threads=1)
+        np.save(result_path, np.array([int(np.array_equal(full, ref)), len(full)]))
+    dist.destroy_process_group()
+
+
+def test_two_rank_sharded_supports_gloo(tmp_path):
+    import socket
+    import torch.multiprocessing as mp
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    out = str(tmp_path / "r.npy")
+    mp.start_processes(_shard_worker, args=(2, port, out), nprocs=2, start_method="spawn")
+    ok, n = np.load(out)
+    assert ok == 1 and n == 1001

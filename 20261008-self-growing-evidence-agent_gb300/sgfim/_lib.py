@@ -102,6 +102,12 @@ SIGNATURES = {
     "sgfim_write_tensorfim": (C.c_int, [C.c_void_p, C.POINTER(Result), C.POINTER(TfMeta), C.c_char_p]),
     "sgfim_write_anyfim": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(Result)), C.POINTER(AfMeta), C.c_char_p]),
     "sgfim_load_scorer": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, u16p, f32p, u16p, f32p, u16p, f32p]),
+    "sgfim_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32] +
+                          [C.c_void_p] * 9 + [C.c_void_p]),
+    "sgfim_mlp_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32] +
+                           [C.c_void_p] * 7 + [C.c_float] + [C.c_void_p] * 7 + [C.c_void_p]),
+    "sgfim_adam_step": (C.c_int, [C.c_void_p] * 6 + [C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float,
+                                                     C.c_uint32, C.c_float, C.c_void_p]),
 }
 
 _lib = None

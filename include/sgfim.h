@@ -257,6 +257,26 @@ int sgfim_load_scorer(sgfim_handle *h, uint32_t in_dim, uint32_t hidden, const u
                       const float *b1, const uint16_t *w2_bf16, const float *b2, const uint16_t *w3_bf16,
                       const float *b3);
 
+/* Training kernels of the scoring MLP (device pointers, asynchronous on
+ * `stream`).  No reference counterpart: the reference has no learned part.
+ * Forward: X [n][in_dim] fp32 -> P [n] probabilities; Z1/Z2 [n][hidden]
+ * receive the pre-activations when non-null.  in_dim 1..64, hidden a
+ * multiple of 32 up to 256. */
+int sgfim_mlp_forward(sgfim_handle *h, const float *X, uint32_t n, uint32_t in_dim, uint32_t hidden,
+                      const uint16_t *W1, const float *b1, const uint16_t *W2, const float *b2, const uint16_t *w3,
+                      const float *b3, float *Z1, float *Z2, float *P, void *stream);
+/* Backward of sum_r scale * WT[r] * BCE(P[r], Y[r]) (WT may be NULL = 1):
+ * gradients are ADDED into dW1 [hidden][in_dim], db1, dW2 [hidden][hidden],
+ * db2, dw3 [hidden], db3 [1]; loss [1] receives the summed loss. */
+int sgfim_mlp_backward(sgfim_handle *h, const float *X, uint32_t n, uint32_t in_dim, uint32_t hidden,
+                       const uint16_t *W2, const uint16_t *w3, const float *Z1, const float *Z2, const float *P,
+                       const float *Y, const float *WT, float scale, float *dW1, float *db1, float *dW2, float *db2,
+                       float *dw3, float *db3, float *loss, void *stream);
+/* One Adam step on fp32 parameters; param_bf16 (nullable) receives the bf16 copy. */
+int sgfim_adam_step(sgfim_handle *h, float *param, const float *grad, float *m, float *v, uint16_t *param_bf16,
+                    uint32_t n, float lr, float beta1, float beta2, float eps, uint32_t step, float weight_decay,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,9 @@
 // and refreshes the bf16 copy after every Adam step.  The layers are small
 // (H = 128): one CTA of H threads owns a tile of rows, thread j owns output
 // column j, and the bf16 weights of layer 2 sit in shared memory.
+#include <cuda_bf16.h>
+
+#include <algorithm>
 #include <cstdio>
 
 #include "common.cuh"

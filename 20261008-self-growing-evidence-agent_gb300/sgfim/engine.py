@@ -238,6 +238,20 @@ class Engine:
             self._L.sgfim_result_free(res)
 
     # ------------------------------------------------------------ scoring
+    def mlp_forward(self, X, n, in_dim, hidden, W1, b1, W2, b2, w3, b3, Z1, Z2, P, stream=0):
+        """Device pointers (ints); see sgfim_mlp_forward."""
+        self._check(self._L.sgfim_mlp_forward(self._h, X, n, in_dim, hidden, W1, b1, W2, b2, w3, b3,
+                                              Z1 or None, Z2 or None, P, stream or None))
+
+    def mlp_backward(self, X, n, in_dim, hidden, W2, w3, Z1, Z2, P, Y, WT, scale, dW1, db1, dW2, db2, dw3, db3,
+                     loss, stream=0):
+        self._check(self._L.sgfim_mlp_backward(self._h, X, n, in_dim, hidden, W2, w3, Z1, Z2, P, Y, WT or None,
+                                               scale, dW1, db1, dW2, db2, dw3, db3, loss, stream or None))
+
+    def adam_step(self, param, grad, m, v, param_bf16, n, lr, beta1, beta2, eps, step, weight_decay, stream=0):
+        self._check(self._L.sgfim_adam_step(self._h, param, grad, m, v, param_bf16 or None, n, lr, beta1, beta2,
+                                            eps, step, weight_decay, stream or None))
+
     def load_scorer(self, w1, b1, w2, b2, w3, b3):
         """Weights as float arrays (converted to bf16 here, round-to-nearest-even)."""
         from .mlp import to_bf16_bits

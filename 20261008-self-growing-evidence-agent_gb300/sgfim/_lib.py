@@ -19,6 +19,8 @@ f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
 
 OK, EINVAL, ENOMEM, EIO, EDEVICE, ESTATE, ETIMEDOUT, ECANCELED, ENODATA = 0, -1, -2, -3, -4, -5, -6, -7, -8
+ECAPACITY = -9
+NOALLOC_MAX_CAND = 1048576
 ROOTS_ALL, ROOTS_LIST, ROOTS_MINCOUNT = 0, 1, 2
 ORDER_SUPPORT, ORDER_LEARNED = 0, 1
 COOC_AUTO, COOC_POPC, COOC_BMMA, COOC_TC_F8 = 0, 1, 2, 3
@@ -92,6 +94,8 @@ SIGNATURES = {
     "sgfim_support_batch_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64,
                                              C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_phase_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PhaseStats), C.c_int]),
+    "sgfim_support_batch_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
+                                              C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),
     "sgfim_cooccurrence_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64,
                                             C.c_void_p, C.c_int, C.c_void_p]),

@@ -45,7 +45,8 @@ enum {
     SGFIM_ESTATE = -5,     /* call out of order (e.g. mining before loading) */
     SGFIM_ETIMEDOUT = -6,  /* the caller's time limit expired */
     SGFIM_ECANCELED = -7,  /* a checkpoint callback asked to stop */
-    SGFIM_ENODATA = -8     /* no transactions loaded */
+    SGFIM_ENODATA = -8,    /* no transactions loaded */
+    SGFIM_ECAPACITY = -9   /* input larger than sgfim_support_batch_noalloc's fixed scratch */
 };
 
 typedef struct sgfim_handle sgfim_handle;
@@ -133,6 +134,28 @@ int sgfim_support_batch_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_
  * equivalent is the b1 AND-POPC GEMM of bmma_bench.cu:99-152 with A = B =
  * the item bitmaps. */
 int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
+
+/* Allocation-free form of sgfim_support_batch_device.  It has no counterpart
+ * in the reference; it exists for callers that must not allocate device
+ * memory: applications whose own memory pool owns the GPU and forbids other
+ * code to call cudaMalloc/cudaFree (for example a serving process that plans
+ * all of its HBM at start-up), or hot loops that cannot afford cudaMalloc's
+ * implicit synchronisation.  It needs no handle and allocates nothing; its
+ * scratch is a fixed array in the library's device memory (about 21 MB, kept
+ * by every GPU that loads the library until the process exits).
+ *   - Arguments and results are those of sgfim_support_batch_device
+ *     (device pointers, asynchronous on `stream`, the current CUDA device).
+ *   - n_cand above SGFIM_NOALLOC_MAX_CAND returns SGFIM_ECAPACITY and does nothing.
+ *   - The first call on a device looks up the array's device address with that
+ *     device current; make that first call before any stream capture.
+ *   - All calls share the one scratch array and it keeps the previous call's
+ *     contents (the kernels clear what they need).  Calls that overlap on the
+ *     GPU -- on different streams or from different host threads -- race on
+ *     it and must be serialised by the caller. */
+#define SGFIM_NOALLOC_MAX_CAND 1048576u
+int sgfim_support_batch_noalloc(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride,
+                                const uint64_t *cand_ptr, const uint32_t *cand_items, uint64_t n_cand,
+                                uint32_t *out, void *stream);
 
 /* Phase timers (CUDA events on the launching stream) of the batched support
  * path, enabled by SGFIM_F_PHASE_TIMERS; the counterpart of the wave engine's

@@ -18,29 +18,9 @@ enum : uint32_t {
     DEVERR_OVERFLOW = 3,       // an output buffer would overflow
 };
 
-#define SG_CUDA_TRY(expr)                                                       \
-    do {                                                                        \
-        cudaError_t e__ = (expr);                                               \
-        if (e__ != cudaSuccess) {                                               \
-            throw sg::CudaError(e__, #expr, __FILE__, __LINE__);               \
-        }                                                                       \
-    } while (0)
+#include "errors.h"
 
 namespace sg {
-
-struct CudaError {
-    cudaError_t code;
-    std::string what;
-    CudaError(cudaError_t c, const char *expr, const char *file, int line) : code(c) {
-        what = std::string(cudaGetErrorString(c)) + " at " + file + ":" + std::to_string(line) + " (" + expr + ")";
-    }
-};
-
-struct EngineError {
-    int code;
-    std::string what;
-    EngineError(int c, std::string w) : code(c), what(std::move(w)) {}
-};
 
 constexpr int kWarp = 32;
 constexpr uint32_t kMbarSpinLimit = 1u << 26;  // ~ seconds of polling; never unbounded

@@ -150,6 +150,7 @@ void sgfim_close(sgfim_handle *h) {
     h->out_dev.release();
     h->dev_err.release();
     h->cooc_scratch.release();
+    h->mws.release();
     h->scorer.w1.release(); h->scorer.b1.release(); h->scorer.w2.release();
     h->scorer.b2.release(); h->scorer.w3.release(); h->scorer.b3.release();
     for (auto &q : h->timer_busy)
@@ -363,7 +364,7 @@ int sgfim_support_batch_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_
     }
     h->support_scratch.reserve(support_scratch_bytes(n_cand), st);
     SupportScratch sc{h->support_scratch.ptr, h->support_scratch.bytes};
-    SupportPlan plan;
+    const SupportPlan &plan = h->plan;
     const uint64_t n_txn = n_words * 64;
     const uint64_t before = h->launches;
     int rc = support_batch_device(bitmaps, d, n_even, row_stride, n_txn, cand_ptr, cand_items, n_cand, out, sc, plan,
@@ -409,7 +410,7 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
                                     h->stream));
     h->support_scratch.reserve(support_scratch_bytes(n_cand), h->stream);
     SupportScratch sc{h->support_scratch.ptr, h->support_scratch.bytes};
-    SupportPlan plan;
+    const SupportPlan &plan = h->plan;
     const uint64_t before = h->launches;
     int rc = support_batch_device(ds.bitmaps.as<uint64_t>(), ds.d, ds.n_words, ds.stride, ds.n_txn,
                                   h->cand_ptr_dev.as<uint64_t>(), h->cand_items_dev.as<uint32_t>(), n_cand,
@@ -424,6 +425,15 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
     SG_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return check_device_error(h);
     API_GUARD_END(h)
+}
+
+int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves) {
+    if (!h) return SGFIM_EINVAL;
+    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_STREAM) return fail(h, SGFIM_EINVAL, "unknown kernel");
+    h->plan.kernel = kernel;
+    h->plan.cands_per_cta = cands_per_cta;
+    h->plan.waves = waves;
+    return SGFIM_OK;
 }
 
 int sgfim_phase_stats_get(sgfim_handle *h, sgfim_phase_stats *out, int reset) {
@@ -460,7 +470,7 @@ int sgfim_cooccurrence_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t
     const size_t sb = cooc_scratch_bytes(d, n_words, kind);
     if (sb) h->cooc_scratch.reserve(sb, st);
     int rc = cooc_device(bitmaps, d, n_words, row_stride, out, kind, st, h->n_sm, h->cooc_scratch.ptr,
-                         h->cooc_scratch.bytes, &h->launches);
+                         h->cooc_scratch.bytes, &h->launches, h->dev_err.as<uint32_t>());
     if (rc) return fail(h, SGFIM_EINVAL, "co-occurrence kernel unavailable for this shape");
     return SGFIM_OK;
     API_GUARD_END(h)
@@ -507,6 +517,8 @@ void sgfim_result_free(sgfim_result *r) {
     free(r->items);
     free(r->support);
     free(r->emit_time_s);
+    free(r->trace_features);
+    free(r->trace_labels);
     free(r);
 }
 

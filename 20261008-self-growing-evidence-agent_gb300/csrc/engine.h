@@ -5,10 +5,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/sgfim.h"
+#include "errors.h"
 #include "kernels.h"
 
 namespace sg {
@@ -54,6 +56,39 @@ struct Dataset {
     std::string source;          // file name or "<memory>"
 };
 
+// A device copy staged through a pinned host buffer (both grow, never shrink).
+struct Staged {
+    DevBuf dev;
+    HostBuf host;
+    template <class T> T *put(const T *src, size_t n, cudaStream_t st) {
+        const size_t b = (n ? n : 1) * sizeof(T);
+        host.reserve(b);
+        dev.reserve(b, st);
+        if (n) {
+            memcpy(host.ptr, src, n * sizeof(T));
+            cudaError_t e = cudaMemcpyAsync(dev.ptr, host.ptr, n * sizeof(T), cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) throw CudaError(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+        }
+        return dev.template as<T>();
+    }
+    void release() { dev.release(); host.release(); }
+};
+
+// Device and pinned buffers of the miner, kept by the handle across calls so
+// that repeated mining (anytime stages, window services) allocates nothing
+// once warm.
+struct MinerWorkspace {
+    DevBuf arena, pool, q_out, score, cooc;
+    HostBuf hq_out, hscore;
+    Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat;
+    void release() {
+        arena.release(); pool.release(); q_out.release(); score.release(); cooc.release();
+        hq_out.release(); hscore.release();
+        for (Staged *s : {&q_ptr, &q_items, &q_slot, &c_ptr, &c_items, &c_ps, &c_cs, &p_ptr, &p_items, &feat})
+            s->release();
+    }
+};
+
 // MLP scorer weights (device) for the learned frontier order.
 struct Scorer {
     bool loaded = false;
@@ -76,6 +111,8 @@ struct sgfim_handle {
     // scratch
     sg::DevBuf support_scratch, cand_ptr_dev, cand_items_dev, out_dev, dev_err;
     sg::DevBuf cooc_scratch;
+    sg::MinerWorkspace mws;
+    sg::SupportPlan plan;
     uint64_t launches = 0;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     // phase timers: event quads recorded by timed calls, resolved by sgfim_phase_stats_get

@@ -46,12 +46,20 @@ void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm);
 // Batched candidate supports (config "support-1m" path).  Packs CSR candidates
 // into 16-byte records when every item fits 16 bits and k <= 8, runs the
 // shared-memory staged kernel on those and the streaming kernel on the rest.
+enum SupportKernel : int { SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3 };
 struct SupportPlan {
-    uint32_t threads = 1024;
+    int kernel = SUPPORT_AUTO;
     uint32_t cands_per_cta = 0;    // 0 = derived from the SM count
-    uint32_t waves = 2;            // CTAs per SM over the whole grid (when cands_per_cta == 0)
-    bool force_stream = false;
+    uint32_t waves = 0;            // CTAs per SM over the grid when cands_per_cta == 0 (0 = kernel default)
 };
+
+// Scratch layout of the support path: records (16 B per candidate), the
+// >8-item list, the sort permutation, the sort bins and a counter word.
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+constexpr size_t kSupportSortBins = 8 * 4096;
+constexpr size_t support_scratch_bytes_for(uint64_t n) {
+    return align256(n * 16) + 2 * align256(n * 4) + align256(kSupportSortBins * 4) + 256;
+}
 struct SupportScratch {
     // device scratch; sized by support_scratch_bytes()
     void *base = nullptr;
@@ -80,7 +88,11 @@ void launch_pool_append(uint64_t *pool_rows, uint64_t pool_stride, const uint64_
 
 // Co-occurrence (d x d) over the bitmap rows.
 int cooc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
-                int kind, cudaStream_t st, int n_sm, void *scratch, size_t scratch_bytes, uint64_t *launches);
+                int kind, cudaStream_t st, int n_sm, void *scratch, size_t scratch_bytes, uint64_t *launches,
+                uint32_t *dev_err = nullptr);
+// tcgen05 e4m3 GEMM form (kernels_tc.cu); returns -1 when the layout is unusable.
+int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
+                   cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches);
 size_t cooc_scratch_bytes(uint32_t d, uint64_t n_words, int kind);
 
 }  // namespace sg

@@ -344,8 +344,231 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// ---------------------------------------------------------------- sorted batch supports
+// Candidates are counting-sorted by key = (k - 1) * 4096 + first item, so that
+// (a) the four 8-lane groups of a warp almost always share k and run one fully
+// unrolled, branch-free K-load AND (unused record slots point at an all-ones
+// row in shared memory), and (b) consecutive candidates of a group usually
+// share their first item, whose 16-byte piece then stays in registers.
+// Sorted record: item0 in bits 0..11 and k in bits 12..15 of .x, items 1..7
+// as 16-bit fields; pad items = the all-ones row index.
+constexpr uint32_t kSortItemMax = 4096;
+constexpr uint32_t kSortBins = 8 * kSortItemMax;
+constexpr uint32_t kSortCompactMax = 1024;  // 10-bit ids in the 12-byte sorted records
+
+__global__ void sort_count_kernel(const uint64_t *__restrict__ cand_ptr, const uint32_t *__restrict__ cand_items,
+                                  uint64_t n, uint32_t d, uint64_t n_txn, uint32_t *__restrict__ bins,
+                                  uint32_t *__restrict__ ovf_list, unsigned long long *__restrict__ ovf_count,
+                                  uint32_t *__restrict__ out) {
+    for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = cand_ptr[c], b = cand_ptr[c + 1];
+        const uint64_t k = b - a;
+        if (k == 0) {
+            out[c] = (uint32_t)n_txn;
+        } else if (k > 8) {
+            ovf_list[atomicAdd(ovf_count, 1ull)] = (uint32_t)c;
+        } else {
+            uint32_t mn = 0xffffffffu;
+            bool zero = false;
+            for (uint64_t i = a; i < b; ++i) {
+                const uint32_t x = cand_items[i];
+                zero |= x >= d;
+                mn = min(mn, x);
+            }
+            if (zero) out[c] = 0;
+            else atomicAdd(&bins[(uint32_t)(k - 1) * kSortItemMax + mn], 1u);
+        }
+    }
+}
+
+// Exclusive scan of the bins in place (one CTA of 1024 threads); total -> *n_valid.
+__global__ void __launch_bounds__(1024) sort_scan_kernel(uint32_t *__restrict__ bins, uint64_t *__restrict__ n_valid) {
+    constexpr uint32_t per = kSortBins / 1024;
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x;
+    uint32_t s = 0;
+    for (uint32_t i = 0; i < per; ++i) s += bins[t * per + i];
+    part[t] = s;
+    __syncthreads();
+    for (uint32_t o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = t ? part[t - 1] : 0u;
+    for (uint32_t i = 0; i < per; ++i) {
+        const uint32_t v = bins[t * per + i];
+        bins[t * per + i] = run;
+        run += v;
+    }
+    if (t == 1023) *n_valid = part[1023];
+}
+
+// Sorted record (12 bytes, ids < 1024): lo = items 0..5 as 10-bit fields and
+// k in bits 60..63; hi = items 6..7 as 10-bit fields.  Slots beyond k repeat
+// item 0 (AND is idempotent), so no padding row is needed.
+__global__ void sort_scatter_kernel(const uint64_t *__restrict__ cand_ptr, const uint32_t *__restrict__ cand_items,
+                                    uint64_t n, uint32_t d, uint32_t *__restrict__ cursor,
+                                    uint64_t *__restrict__ rec_lo, uint32_t *__restrict__ rec_hi,
+                                    uint32_t *__restrict__ perm) {
+    for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = cand_ptr[c], b = cand_ptr[c + 1];
+        const uint64_t k = b - a;
+        if (k == 0 || k > 8) continue;
+        uint32_t it[8];
+        uint32_t mn = 0xffffffffu, at = 0;
+        bool zero = false;
+        for (uint64_t i = a; i < b; ++i) {
+            const uint32_t x = cand_items[i];
+            zero |= x >= d;
+            if (x < mn) { mn = x; at = (uint32_t)(i - a); }
+            it[i - a] = x;
+        }
+        if (zero) continue;
+        // the smallest item goes first (it is the sort key and the reused row)
+        it[at] = it[0];
+        it[0] = mn;
+        for (uint64_t i = k; i < 8; ++i) it[i] = mn;
+        const uint32_t pos = atomicAdd(&cursor[(uint32_t)(k - 1) * kSortItemMax + mn], 1u);
+        uint64_t lo = (uint64_t)k << 60;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) lo |= (uint64_t)it[i] << (10 * i);
+        rec_lo[pos] = lo;
+        rec_hi[pos] = it[6] | (it[7] << 10);
+        perm[pos] = (uint32_t)c;
+    }
+}
+
+__device__ __forceinline__ uint32_t rec_item(uint64_t lo, uint32_t hi, int i) {
+    return i < 6 ? (uint32_t)(lo >> (10 * i)) & 1023u : (hi >> (10 * (i - 6))) & 1023u;
+}
+
+template <int K>
+__device__ __forceinline__ uint4 and_tail(const uint8_t *base, uint64_t lo, uint32_t hi, uint4 m) {
+#pragma unroll
+    for (int i = 1; i < K; ++i) m = and4(m, *reinterpret_cast<const uint4 *>(base + (size_t)rec_item(lo, hi, i) * 128));
+    return m;
+}
+
+// Same chunk pipeline as k1_staged_kernel.  Group g owns a contiguous run of
+// the CTA's sorted candidates, so consecutive candidates usually share k
+// (one unrolled K-load AND per warp, K = the warp's largest k) and their
+// first item, whose 16-byte piece stays in registers.  Slots past a group's
+// run issue no shared loads.
+template <int THREADS, int SMAX>
+__global__ void __launch_bounds__(THREADS, 1)
+    k1_sorted_kernel(const __grid_constant__ CUtensorMap bm_map, uint32_t n_boxes, uint64_t n_words,
+                     const uint64_t *__restrict__ rec_lo, const uint32_t *__restrict__ rec_hi,
+                     const uint32_t *__restrict__ perm, const uint64_t *__restrict__ n_valid, uint32_t cpc,
+                     uint32_t *__restrict__ out, uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr uint32_t G = THREADS / 8;
+    const uint32_t chunk_bytes = n_boxes * kStagedRowsPerBox * kStagedWords * 8;
+    uint8_t *chunk = smem;
+    uint64_t *lo_s = reinterpret_cast<uint64_t *>(smem + chunk_bytes);
+    uint32_t *hi_s = reinterpret_cast<uint32_t *>(lo_s + cpc);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + chunk_bytes + (size_t)cpc * 12 + 16 - ((size_t)cpc * 12) % 16);
+
+    const uint32_t tid = threadIdx.x, g = tid >> 3, l = tid & 7;
+    const uint64_t nv = *n_valid;
+    const uint64_t base = (uint64_t)blockIdx.x * cpc;
+    if (base >= nv) return;
+    const uint32_t ncta = (uint32_t)min((uint64_t)cpc, nv - base);
+    const uint32_t per_g = (ncta + G - 1) / G;
+    const uint32_t g_lo = min(g * per_g, ncta), g_hi = min(g_lo + per_g, ncta);
+    const uint32_t n_sets = (per_g + 7) / 8;
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    for (uint32_t i = tid; i < ncta; i += THREADS) {
+        lo_s[i] = rec_lo[base + i];
+        hi_s[i] = rec_hi[base + i];
+    }
+    __syncthreads();
+
+    uint32_t acc[SMAX];
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) acc[s] = 0;
+    const uint64_t n_chunks = (n_words + kStagedWords - 1) / kStagedWords;
+    const uint8_t *lane_base = chunk + l * 16;
+    uint32_t phase = 0;
+    for (uint64_t ch = 0; ch < n_chunks; ++ch) {
+        if (tid == 0) {
+            mbar_arrive_expect_tx(bar, chunk_bytes);
+            for (uint32_t b = 0; b < n_boxes; ++b)
+                tma_load_2d(chunk + (size_t)b * kStagedRowsPerBox * kStagedWords * 8, &bm_map,
+                            (int32_t)(ch * kStagedWords), (int32_t)(b * kStagedRowsPerBox), bar);
+        }
+        const bool ok = mbar_wait_bounded(bar, phase, err);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            mbar_wait_bounded(bar, phase ^ 1, err);
+            return;
+        }
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s) {
+            if ((uint32_t)s < n_sets) {
+                uint32_t p[8];
+                uint32_t cur0 = 0xffffffffu;
+                uint4 row0 = make_uint4(0, 0, 0, 0);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const uint32_t c = g_lo + (uint32_t)s * 8 + j;
+                    const bool valid = c < g_hi;
+                    uint64_t lo = 0;
+                    uint32_t hi = 0;
+                    if (valid) {
+                        lo = lo_s[c];
+                        hi = hi_s[c];
+                    }
+                    const uint32_t k = (uint32_t)(lo >> 60);
+                    const uint32_t kmax = __reduce_max_sync(0xffffffffu, k);
+                    uint32_t v = 0;
+                    if (valid) {
+                        const uint32_t it0 = (uint32_t)lo & 1023u;
+                        if (it0 != cur0) {
+                            row0 = *reinterpret_cast<const uint4 *>(lane_base + (size_t)it0 * 128);
+                            cur0 = it0;
+                        }
+                        uint4 m = row0;
+                        switch (kmax) {
+                            case 2: m = and_tail<2>(lane_base, lo, hi, m); break;
+                            case 3: m = and_tail<3>(lane_base, lo, hi, m); break;
+                            case 4: m = and_tail<4>(lane_base, lo, hi, m); break;
+                            case 5: m = and_tail<5>(lane_base, lo, hi, m); break;
+                            case 6: m = and_tail<6>(lane_base, lo, hi, m); break;
+                            case 7: m = and_tail<7>(lane_base, lo, hi, m); break;
+                            case 8: m = and_tail<8>(lane_base, lo, hi, m); break;
+                            default: break;
+                        }
+                        v = popc4(m);
+                    }
+                    p[j] = v;
+                }
+                acc[s] += treduce8(p, l);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) {
+        const uint32_t c = g_lo + (uint32_t)s * 8 + l;
+        if ((uint32_t)s < n_sets && c < g_hi) out[perm[base + c]] = acc[s];
+    }
+}
+
 constexpr int kStagedThreads = 1024;
 constexpr int kStagedSmax = 8;
+constexpr int kSortedSmax = 8;
+constexpr uint32_t kSortedMaxCpc = kStagedThreads / 8 * 8 * kSortedSmax;  // 8192
+
+size_t sorted_smem_bytes(uint32_t d, uint32_t cpc) {
+    const uint32_t n_boxes = (d + kStagedRowsPerBox - 1) / kStagedRowsPerBox;
+    return (size_t)n_boxes * kStagedRowsPerBox * kStagedWords * 8 + (size_t)cpc * 12 + 16 + 64;
+}
 constexpr uint32_t kStagedMaxCpc = kStagedThreads / 8 * 8 * kStagedSmax;  // 8192
 
 size_t staged_smem_bytes(uint32_t d, uint32_t cpc) {
@@ -378,11 +601,7 @@ bool encode_bitmap_map(CUtensorMap *map, const uint64_t *bitmaps, uint32_t d, ui
     return r == CUDA_SUCCESS;
 }
 
-static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-size_t support_scratch_bytes(uint64_t n_cand) {
-    return align_up(n_cand * 16, 256) + align_up(n_cand * 4, 256) + 256;
-}
+size_t support_scratch_bytes(uint64_t n_cand) { return support_scratch_bytes_for(n_cand); }
 
 int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride,
                          uint64_t n_txn, const uint64_t *cand_ptr, const uint32_t *cand_items, uint64_t n_cand,
@@ -394,19 +613,32 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
         if (ev) SG_CUDA_TRY(cudaEventRecord(ev[i], st));
     };
     const uint64_t n_words_even = (n_words + 1) & ~1ull;
-    bool staged = !plan.force_stream && map != nullptr && d <= 65535 && d > 0;
-    uint32_t cpc = plan.cands_per_cta;
-    if (staged) {
-        if (cpc == 0) {
-            const uint64_t ctas = (uint64_t)n_sm * std::max<uint32_t>(1, plan.waves);
-            cpc = (uint32_t)std::min<uint64_t>(kStagedMaxCpc, (n_cand + ctas - 1) / ctas);
-            cpc = std::max<uint32_t>(cpc, 1);
-        }
-        cpc = std::min(cpc, kStagedMaxCpc);
-        while (cpc > 1 && staged_smem_bytes(d, cpc) > 227 * 1024) cpc = cpc * 3 / 4;
-        if (staged_smem_bytes(d, cpc) > 227 * 1024) staged = false;
+    // default grid: one wave of CTAs for the sorted kernel (its 12-byte records leave room
+    // for ~6,600 candidates per CTA), two for the staged kernel
+    auto pick_cpc = [&](uint32_t cap, size_t (*smem_fn)(uint32_t, uint32_t), uint32_t waves) -> uint32_t {
+        const uint64_t ctas_target = (uint64_t)n_sm * std::max<uint32_t>(1, plan.waves ? plan.waves : waves);
+        uint32_t cpc = plan.cands_per_cta;
+        if (cpc == 0) cpc = (uint32_t)std::min<uint64_t>(cap, (n_cand + ctas_target - 1) / ctas_target);
+        cpc = std::max<uint32_t>(1, std::min(cpc, cap));
+        while (cpc > 1 && smem_fn(d, cpc) > 227 * 1024) cpc = cpc * 3 / 4;
+        return smem_fn(d, cpc) <= 227 * 1024 ? cpc : 0;
+    };
+    int kind = plan.kernel;
+    if (map == nullptr || d == 0) kind = SUPPORT_STREAM;
+    // measured on GB300 at 1M candidates x 1,024 rows: staged 30.9 ms, sorted 30.8-46 ms
+    // (depending on its grid); the staged kernel is the default, the sorted one a tuning option
+    if (kind == SUPPORT_AUTO) kind = SUPPORT_STAGED;
+    if (kind == SUPPORT_SORTED && d > kSortCompactMax) kind = SUPPORT_STAGED;
+    if (kind == SUPPORT_STAGED && d > 65535) kind = SUPPORT_STREAM;
+    uint32_t cpc = 0;
+    if (kind == SUPPORT_SORTED) {
+        cpc = pick_cpc(kSortedMaxCpc, sorted_smem_bytes, 1);
+        if (!cpc) kind = SUPPORT_STREAM;
+    } else if (kind == SUPPORT_STAGED) {
+        cpc = pick_cpc(kStagedMaxCpc, staged_smem_bytes, 2);
+        if (!cpc) kind = SUPPORT_STREAM;
     }
-    if (!staged) {
+    if (kind == SUPPORT_STREAM) {
         QueryBatch qb;
         qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;
         qb.q_ptr = cand_ptr; qb.q_items = cand_items; qb.n_q = n_cand; qb.out = out; qb.empty_value = n_txn;
@@ -421,23 +653,50 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     if (scratch.bytes < support_scratch_bytes(n_cand)) return -1;
     uint8_t *sb = static_cast<uint8_t *>(scratch.base);
     uint4 *recs = reinterpret_cast<uint4 *>(sb);
-    uint32_t *ovf = reinterpret_cast<uint32_t *>(sb + align_up(n_cand * 16, 256));
-    unsigned long long *ovf_n =
-        reinterpret_cast<unsigned long long *>(sb + align_up(n_cand * 16, 256) + align_up(n_cand * 4, 256));
+    uint32_t *ovf = reinterpret_cast<uint32_t *>(sb + align256(n_cand * 16));
+    uint32_t *perm = reinterpret_cast<uint32_t *>(sb + align256(n_cand * 16) + align256(n_cand * 4));
+    uint32_t *bins = reinterpret_cast<uint32_t *>(sb + align256(n_cand * 16) + 2 * align256(n_cand * 4));
+    unsigned long long *ovf_n = reinterpret_cast<unsigned long long *>(
+        sb + align256(n_cand * 16) + 2 * align256(n_cand * 4) + align256(kSupportSortBins * 4));
+    uint64_t *n_valid = reinterpret_cast<uint64_t *>(ovf_n + 1);
+    const uint32_t n_boxes = (d + kStagedRowsPerBox - 1) / kStagedRowsPerBox;
+    const unsigned prep_blocks = (unsigned)std::min<uint64_t>((n_cand + 255) / 256, (uint64_t)n_sm * 16);
+    const uint64_t ctas = (n_cand + cpc - 1) / cpc;
     mark(0);
     SG_CUDA_TRY(cudaMemsetAsync(ovf_n, 0, 8, st));
-    const unsigned prep_blocks = (unsigned)std::min<uint64_t>((n_cand + 255) / 256, (uint64_t)n_sm * 16);
-    prep_records_kernel<<<prep_blocks, 256, 0, st>>>(cand_ptr, cand_items, n_cand, d, n_txn, recs, ovf, ovf_n, out);
-    SG_CUDA_TRY(cudaGetLastError());
-    const uint32_t n_boxes = (d + kStagedRowsPerBox - 1) / kStagedRowsPerBox;
-    const size_t smem = staged_smem_bytes(d, cpc);
-    auto kern = k1_staged_kernel<kStagedThreads, kStagedSmax>;
-    SG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const uint64_t ctas = (n_cand + cpc - 1) / cpc;
-    mark(1);
-    kern<<<(unsigned)ctas, kStagedThreads, smem, st>>>(*map, n_boxes, n_words_even, recs, n_cand, cpc, out, dev_err);
-    SG_CUDA_TRY(cudaGetLastError());
-    mark(2);
+    if (kind == SUPPORT_SORTED) {
+        SG_CUDA_TRY(cudaMemsetAsync(bins, 0, kSupportSortBins * 4, st));
+        sort_count_kernel<<<prep_blocks, 256, 0, st>>>(cand_ptr, cand_items, n_cand, d, n_txn, bins, ovf, ovf_n, out);
+        SG_CUDA_TRY(cudaGetLastError());
+        sort_scan_kernel<<<1, 1024, 0, st>>>(bins, n_valid);
+        SG_CUDA_TRY(cudaGetLastError());
+        uint64_t *rec_lo = reinterpret_cast<uint64_t *>(recs);
+        uint32_t *rec_hi = reinterpret_cast<uint32_t *>(rec_lo + n_cand);
+        sort_scatter_kernel<<<prep_blocks, 256, 0, st>>>(cand_ptr, cand_items, n_cand, d, bins, rec_lo, rec_hi, perm);
+        SG_CUDA_TRY(cudaGetLastError());
+        const size_t smem = sorted_smem_bytes(d, cpc);
+        auto kern = k1_sorted_kernel<kStagedThreads, kSortedSmax>;
+        SG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        mark(1);
+        kern<<<(unsigned)ctas, kStagedThreads, smem, st>>>(*map, n_boxes, n_words_even, rec_lo, rec_hi, perm, n_valid,
+                                                           cpc, out, dev_err);
+        SG_CUDA_TRY(cudaGetLastError());
+        mark(2);
+        if (launches) *launches += 4;
+    } else {
+        prep_records_kernel<<<prep_blocks, 256, 0, st>>>(cand_ptr, cand_items, n_cand, d, n_txn, recs, ovf, ovf_n,
+                                                         out);
+        SG_CUDA_TRY(cudaGetLastError());
+        const size_t smem = staged_smem_bytes(d, cpc);
+        auto kern = k1_staged_kernel<kStagedThreads, kStagedSmax>;
+        SG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        mark(1);
+        kern<<<(unsigned)ctas, kStagedThreads, smem, st>>>(*map, n_boxes, n_words_even, recs, n_cand, cpc, out,
+                                                           dev_err);
+        SG_CUDA_TRY(cudaGetLastError());
+        mark(2);
+        if (launches) *launches += 2;
+    }
     // candidates with more than 8 items
     QueryBatch qb;
     qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;
@@ -445,7 +704,7 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     qb.q_index = ovf; qb.out = out; qb.empty_value = n_txn;
     launch_queries(qb, st, n_sm);
     mark(3);
-    if (launches) *launches += 3;
+    if (launches) *launches += 1;
     return 0;
 }
 

@@ -1,0 +1,238 @@
+// kernels_tc.cu -- co-occurrence on the 5th-generation tensor cores (tcgen05).
+//
+// C[i][j] = popc(bv_i & bv_j) is the dot product of two 0/1 vectors.  Bits
+// are expanded to fp8 e4m3 bytes (1.0 = 0x38, 0.0 = 0x00; both exact) inside
+// the kernel and multiplied with tcgen05.mma .kind::f8f6f4, accumulating in
+// fp32 in tensor memory: every partial sum is an integer below 2^24 (a CTA
+// covers at most 2^20 transactions per split), so fp32 holds it exactly.
+// The reference does this product with b1 AND-POPC wmma fragments
+// (code/engine_tensorfim/code/microbench/bmma_bench.cu:99-152); GB300 has no
+// b1 tcgen05 kind and its int8 tensor rate is cut, hence e4m3.
+//
+// Tiling: a CTA owns one upper-triangle 128 x 128 tile (rows bi, columns bj)
+// and a slice of the transactions.  Per stage, 256 threads expand a 256-bit
+// slice of 128 + 128 rows into two 128B-swizzled K-major atoms per operand
+// (row r, byte b at r*128 + ((b/16) ^ (r%8))*16 + b%16), fence the async
+// proxy, and one thread issues 8 MMAs of K=32; tcgen05.commit arrives on the
+// stage's mbarrier when the tensor core is done reading it.  The epilogue
+// reads the 128 x 128 fp32 accumulator from TMEM (tcgen05.ld 32x32b) and
+// adds the integer counts into C (and its mirror) with atomics.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sg {
+
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcStages = 3;
+constexpr int kTcAtom = 128 * 128;             // one 128-row x 128-byte swizzle atom
+constexpr int kTcOperand = 2 * kTcAtom;        // two atoms along K per operand
+constexpr int kTcStageBytes = 2 * kTcOperand;  // A and B
+constexpr uint32_t kTcCols = 128;              // TMEM columns (fp32 accumulators)
+
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    // sm_100 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading
+    // byte offset >> 4 (16-29, unused for swizzled K-major: 1), stride byte
+    // offset >> 4 (32-45: 1024 B between 8-row groups), version 1 (46-47),
+    // base offset 0 (49-51), layout SWIZZLE_128B = 2 (61-63).
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3fff);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor, kind::f8f6f4: D = f32 (bits 4-5 = 1), A = B = e4m3
+// (bits 7-9, 10-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kTcIdesc = (1u << 4) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+// 4 bits -> 4 bytes of e4m3 (0x38 = 1.0 where the bit is set).
+__device__ __forceinline__ uint32_t nib4(uint32_t n) { return ((n * 0x00204081u) & 0x01010101u) * 0x38u; }
+
+// Expand 128 bits (two u64) into one 128-byte swizzled row of an atom.
+__device__ __forceinline__ void expand_row(uint8_t *atom, uint32_t r, uint64_t lo, uint64_t hi) {
+    uint8_t *row = atom + r * 128;
+    const uint32_t x = r & 7;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint64_t w = c < 4 ? lo : hi;
+        const uint32_t bits = (uint32_t)(w >> ((c & 3) * 16)) & 0xffffu;
+        const uint4 v = make_uint4(nib4(bits & 15), nib4((bits >> 4) & 15), nib4((bits >> 8) & 15), nib4(bits >> 12));
+        *reinterpret_cast<uint4 *>(row + ((c ^ x) << 4)) = v;
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    cooc_tc_kernel(const uint64_t *__restrict__ bm, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t n_tiles,
+                   uint64_t words_per_split, uint32_t *__restrict__ out, uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bars[kTcStages + 1];
+    __shared__ uint32_t tmem_slot;
+    uint32_t t = blockIdx.x, bi = 0;
+    while (t >= n_tiles - bi) { t -= n_tiles - bi; ++bi; }
+    const uint32_t bj = bi + t;
+    const uint64_t w_begin = (uint64_t)blockIdx.y * words_per_split;
+    const uint64_t w_end = min(n_words, w_begin + words_per_split);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    // 1024-byte aligned stage base (SWIZZLE_128B atoms)
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem) + 1023) & ~uintptr_t(1023));
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s <= kTcStages; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    const uint64_t n_steps = w_begin < w_end ? (w_end - w_begin + 3) / 4 : 0;  // 4 words = 256 bits per step
+    bool ok = true;
+    for (uint64_t it = 0; it < n_steps; ++it) {
+        const uint32_t s = (uint32_t)(it % kTcStages);
+        uint8_t *stage = base + (size_t)s * kTcStageBytes;
+        if (it >= kTcStages) {
+            // the MMAs that read this stage kStages steps ago must be done
+            ok = mbar_wait_bounded(&bars[s], (uint32_t)((it / kTcStages - 1) & 1), err);
+        }
+        if (__syncthreads_or(!ok)) break;
+        // expand: thread -> one row of A (tid < 128) or B (tid >= 128), 256 bits
+        {
+            const uint32_t r = tid & 127;
+            const uint32_t row = (tid < 128 ? bi : bj) * 128 + r;
+            uint8_t *op = stage + (tid < 128 ? 0 : kTcOperand);
+            const uint64_t w0 = w_begin + it * 4;
+            uint64_t v[4] = {0, 0, 0, 0};
+            if (row < d) {
+                const uint64_t *src = bm + (uint64_t)row * stride + w0;
+                if (w0 + 3 < w_end) {
+                    const uint4 a = ld_nc_v4(src), b = ld_nc_v4(src + 2);
+                    v[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
+                    v[1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
+                    v[2] = (uint64_t)b.x | ((uint64_t)b.y << 32);
+                    v[3] = (uint64_t)b.z | ((uint64_t)b.w << 32);
+                } else {
+                    for (int q = 0; q < 4; ++q)
+                        if (w0 + q < w_end) v[q] = src[q];
+                }
+            }
+            expand_row(op, r, v[0], v[1]);
+            expand_row(op + kTcAtom, r, v[2], v[3]);
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_addr(stage), b0 = smem_addr(stage + kTcOperand);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t off = (uint32_t)(k >> 2) * kTcAtom + (uint32_t)(k & 3) * 32;
+                tc_mma(tmem, smem_desc_sw128(a0 + off), smem_desc_sw128(b0 + off), (it > 0 || k > 0) ? 1u : 0u);
+            }
+            tc_commit(&bars[s]);
+        }
+    }
+    // wait for every MMA before reading the accumulator
+    if (tid == 0) {
+        if (n_steps > 0) tc_commit(&bars[kTcStages]);
+    }
+    __syncthreads();
+    if (ok && n_steps > 0) ok = mbar_wait_bounded(&bars[kTcStages], 0, err);
+    tc_fence_after();
+    if (__syncthreads_or(!ok) == 0 && n_steps > 0 && warp < 4) {
+        const uint32_t lane_base = warp * 32;
+        const uint32_t row = bi * 128 + lane_base + (tid & 31);
+#pragma unroll 1
+        for (uint32_t cb = 0; cb < kTcCols; cb += 32) {
+            uint32_t v[32];
+            const uint32_t taddr = tmem + (lane_base << 16) + cb;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < d) {
+#pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                    const uint32_t col = bj * 128 + cb + q;
+                    const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
+                    if (col < d && cnt) {
+                        atomicAdd(&out[(uint64_t)row * d + col], cnt);
+                        if (bi != bj) atomicAdd(&out[(uint64_t)col * d + row], cnt);
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+    }
+}
+
+}  // namespace
+
+size_t tc_smem_bytes() { return (size_t)kTcStages * kTcStageBytes + 1024; }
+
+int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
+                   cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches) {
+    if (d == 0) return 0;
+    if ((reinterpret_cast<uintptr_t>(bitmaps) & 15) || (row_stride & 1)) return -1;
+    SG_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)d * d * 4, st));
+    const uint32_t n_tiles = (d + 127) / 128;
+    const uint32_t pairs = n_tiles * (n_tiles + 1) / 2;
+    // one wave: split the transactions so that pairs x splits <= SMs; each split
+    // covers at most 2^20 transactions (fp32 exactness of the partial counts)
+    uint64_t splits = std::max<uint64_t>(1, (uint64_t)n_sm / pairs);
+    uint64_t wps = (n_words + splits - 1) / splits;
+    wps = std::min<uint64_t>(wps, (1ull << 20) / 64);
+    wps = (wps + 3) / 4 * 4;
+    splits = (n_words + wps - 1) / wps;
+    const size_t smem = tc_smem_bytes();
+    SG_CUDA_TRY(cudaFuncSetAttribute(cooc_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(pairs, (unsigned)splits);
+    cooc_tc_kernel<<<grid, kTcThreads, smem, st>>>(bitmaps, row_stride, n_words, d, n_tiles, wps, out, dev_err);
+    SG_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 1;
+    return 0;
+}
+
+}  // namespace sg

@@ -9,7 +9,7 @@
 //   node (H, T):   s_e = sup(H u {e}) for e in T, counted on the device from H's
 //                  tidset mask (one batched launch per wave of nodes)
 //   PEP:           e with s_e == sup(H) joins H (same tidset)
-//   order:         the remaining frequent tail F sorted by ascending support
+//   tail order:    the remaining frequent tail F sorted by ascending support
 //   leaf:          F empty -> H is a candidate unless a pool member contains it
 //   HUT:           H u F contained in a pool member -> no new MFI below
 //   FHUT:          sup(H u F) >= thr -> H u F is the subtree's only candidate
@@ -18,32 +18,41 @@
 // The pool of candidates lives on the device as a vertical bitmap (one bit
 // per candidate in every item's row), so "is Q contained in a candidate" is an
 // AND-popcount query over the pool rows -- the same kernel as support counting.
-// Candidates emitted in one wave are not tested against each other, so the
-// final maximality filter counts, for every candidate, the pool members that
-// contain it; exactly one (itself) means the candidate is maximal.
+// Candidates are tested against the pool as it stood when they were found, so
+// the final maximality filter counts, for every candidate, the pool members
+// that contain it; exactly one (itself) means the candidate is maximal.
+//
+// The order in which sibling subtrees are searched is a policy (canonical
+// ascending support, support descending, or the learned scorer); the tree,
+// every count and the final set do not depend on it.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
-#include <queue>
 
 #include "common.cuh"
 #include "engine.h"
 
 namespace sg {
 
+void launch_mlp_forward(const float *X, uint32_t n, uint32_t F, uint32_t H, const uint16_t *W1, const float *b1,
+                        const uint16_t *W2, const float *b2, const uint16_t *w3, const float *b3, float *Z1,
+                        float *Z2, float *P, cudaStream_t st);
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr uint32_t kNoNode = 0xffffffffu;
+constexpr uint32_t kDim = SGFIM_TRACE_DIM;
 
 struct MNode {
     std::vector<uint32_t> head;  // dense ids
-    std::vector<uint32_t> tail;  // dense ids, search order
+    std::vector<uint32_t> tail;  // dense ids, ascending support
     uint32_t sup = 0;
     uint32_t slot = kNoSlot;     // tidset mask slot; kNoSlot = AND of head rows
-    float prio = 0.f;
+    uint32_t id = 0;             // search-tree node id
 };
 
 struct QuerySet {
@@ -61,12 +70,11 @@ struct QuerySet {
 
 class Miner {
   public:
-    Miner(sgfim_handle *h, const sgfim_mine_params &p) : h_(h), ds_(h->ds), p_(p) {}
-    ~Miner() {
-        arena_.release(); pool_.release();
-        dq_ptr_.release(); dq_items_.release(); dq_slot_.release(); dq_out_.release();
-        hq_ptr_.release(); hq_items_.release(); hq_slot_.release(); hq_out_.release();
-    }
+    Miner(sgfim_handle *h, const sgfim_mine_params &p)
+        : h_(h), ds_(h->ds), p_(p), w_(h->mws), arena_(w_.arena), pool_(w_.pool), q_ptr_(w_.q_ptr),
+          q_items_(w_.q_items), q_slot_(w_.q_slot), c_ptr_(w_.c_ptr), c_items_(w_.c_items), c_ps_(w_.c_ps),
+          c_cs_(w_.c_cs), p_ptr_(w_.p_ptr), p_items_(w_.p_items), feat_(w_.feat), q_out_(w_.q_out),
+          score_(w_.score), hq_out_(w_.hq_out), hscore_(w_.hscore) {}
 
     int run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out);
 
@@ -74,24 +82,33 @@ class Miner {
     sgfim_handle *h_;
     Dataset &ds_;
     sgfim_mine_params p_;
+    MinerWorkspace &w_;
     uint32_t thr_ = 1;
     Clock::time_point t0_;
-    // tidset masks
-    DevBuf arena_;
+    // tidset masks (slots of the workspace arena)
+    DevBuf &arena_;
     uint64_t slot_words_ = 0;
     std::vector<uint32_t> free_slots_;
-    // device pool (rows = items, one bit per candidate)
-    DevBuf pool_;
-    uint64_t pool_words_ = 0;   // words per pool row (capacity / 64)
-    uint64_t pool_n_ = 0;       // members in the device pool
+    // device pool (rows = items, one bit per candidate), in the workspace
+    DevBuf &pool_;
+    uint64_t pool_words_ = 0;
+    uint64_t pool_n_ = 0;
     // candidates (host)
     std::vector<uint64_t> cptr_{0};
     std::vector<uint32_t> citems_;
     std::vector<uint32_t> csup_;
     std::vector<double> ctime_;
-    // query staging
-    DevBuf dq_ptr_, dq_items_, dq_slot_, dq_out_;
-    HostBuf hq_ptr_, hq_items_, hq_slot_, hq_out_;
+    std::vector<uint32_t> cnode_;
+    // search tree and trace
+    std::vector<uint32_t> parent_;
+    std::vector<float> tfeat_;
+    std::vector<uint32_t> tnode_;
+    bool need_feat_ = false;
+    std::vector<uint32_t> cooc_;
+    // staging (workspace)
+    Staged &q_ptr_, &q_items_, &q_slot_, &c_ptr_, &c_items_, &c_ps_, &c_cs_, &p_ptr_, &p_items_, &feat_;
+    DevBuf &q_out_, &score_;
+    HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
 
     double elapsed() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
@@ -104,8 +121,12 @@ class Miner {
     void run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
                      int mode, std::vector<uint32_t> &out);
     void pool_reserve(uint64_t members);
-    void emit(const std::vector<uint32_t> &set, uint32_t sup);
+    void emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node);
     void flush_pool(uint64_t from);
+    void load_cooc();
+    void features(const std::vector<uint32_t> &head, uint32_t head_sup, uint32_t e, uint32_t s, uint32_t pos,
+                  uint32_t nf, float *f) const;
+    void score(const std::vector<float> &feat, size_t n, std::vector<float> &out);
     int finish(sgfim_result **out);
 };
 
@@ -115,38 +136,37 @@ void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t strid
     out.assign(n, 0);
     if (n == 0) return;
     cudaStream_t st = h_->stream;
-    hq_ptr_.reserve((n + 1) * 8);
-    hq_items_.reserve(std::max<size_t>(qs.items.size(), 1) * 4);
-    hq_slot_.reserve(n * 4);
-    hq_out_.reserve(n * 4);
-    memcpy(hq_ptr_.ptr, qs.ptr.data(), (n + 1) * 8);
-    if (!qs.items.empty()) memcpy(hq_items_.ptr, qs.items.data(), qs.items.size() * 4);
-    memcpy(hq_slot_.ptr, qs.slot.data(), n * 4);
-    dq_ptr_.reserve((n + 1) * 8, st);
-    dq_items_.reserve(std::max<size_t>(qs.items.size(), 1) * 4, st);
-    dq_slot_.reserve(n * 4, st);
-    dq_out_.reserve(n * 4, st);
-    SG_CUDA_TRY(cudaMemcpyAsync(dq_ptr_.ptr, hq_ptr_.ptr, (n + 1) * 8, cudaMemcpyHostToDevice, st));
-    if (!qs.items.empty())
-        SG_CUDA_TRY(cudaMemcpyAsync(dq_items_.ptr, hq_items_.ptr, qs.items.size() * 4, cudaMemcpyHostToDevice, st));
-    SG_CUDA_TRY(cudaMemcpyAsync(dq_slot_.ptr, hq_slot_.ptr, n * 4, cudaMemcpyHostToDevice, st));
     QueryBatch qb;
+    qb.q_ptr = q_ptr_.put(qs.ptr.data(), n + 1, st);
+    qb.q_items = q_items_.put(qs.items.data(), qs.items.size(), st);
+    qb.mask_slot = q_slot_.put(qs.slot.data(), n, st);
+    q_out_.reserve(n * 4, st);
+    hq_out_.reserve(n * 4);
     qb.rows = rows; qb.row_stride = stride; qb.n_words = n_words; qb.d = d;
-    qb.q_ptr = dq_ptr_.as<uint64_t>(); qb.q_items = dq_items_.as<uint32_t>();
-    qb.mask_slot = dq_slot_.as<uint32_t>(); qb.arena = arena_.as<uint64_t>(); qb.arena_stride = slot_words_;
-    qb.n_q = n; qb.out = dq_out_.as<uint32_t>(); qb.empty_value = ds_.n_txn; qb.mode = mode;
+    qb.arena = arena_.as<uint64_t>(); qb.arena_stride = slot_words_;
+    qb.n_q = n; qb.out = q_out_.as<uint32_t>(); qb.empty_value = ds_.n_txn; qb.mode = mode;
     launch_queries(qb, st, h_->n_sm);
     ++launches_;
-    SG_CUDA_TRY(cudaMemcpyAsync(hq_out_.ptr, dq_out_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(hq_out_.ptr, q_out_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
     SG_CUDA_TRY(cudaStreamSynchronize(st));
     memcpy(out.data(), hq_out_.ptr, n * 4);
 }
 
+// Grow the pool to hold `members` candidates.  The workspace buffer may be
+// larger than one row layout needs (left over from an earlier call): the
+// layout uses as many words per row as fit.
 void Miner::pool_reserve(uint64_t members) {
     const uint64_t need_words = ((members + 63) / 64 + 1) & ~1ull;
     if (need_words <= pool_words_) return;
+    const size_t row_bytes_have = pool_.bytes / std::max<uint32_t>(ds_.d, 1);
     uint64_t nw = std::max<uint64_t>(need_words, std::max<uint64_t>(pool_words_ * 2, 1024));
     nw = (nw + 1) & ~1ull;
+    if (pool_words_ == 0 && (size_t)nw * 8 <= row_bytes_have) {
+        // first use in this call: adopt the existing buffer, cleared
+        pool_words_ = (row_bytes_have / 8) & ~1ull;
+        SG_CUDA_TRY(cudaMemsetAsync(pool_.ptr, 0, (size_t)ds_.d * pool_words_ * 8, h_->stream));
+        return;
+    }
     void *np = nullptr;
     SG_CUDA_TRY(cudaMalloc(&np, (size_t)ds_.d * nw * 8));
     SG_CUDA_TRY(cudaMemsetAsync(np, 0, (size_t)ds_.d * nw * 8, h_->stream));
@@ -160,16 +180,18 @@ void Miner::pool_reserve(uint64_t members) {
     pool_words_ = nw;
 }
 
-void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup) {
+void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node) {
     std::vector<uint32_t> s(set);
     std::sort(s.begin(), s.end());
     citems_.insert(citems_.end(), s.begin(), s.end());
     cptr_.push_back(citems_.size());
     csup_.push_back(sup);
     ctime_.push_back(elapsed());
+    cnode_.push_back(node);
 }
 
-// Append candidates [from, n) to the device pool.
+// Append candidates [from, n) to the device pool (asynchronous; the next
+// query synchronises the stream before the staging buffers are reused).
 void Miner::flush_pool(uint64_t from) {
     const uint64_t n = csup_.size();
     if (from >= n) return;
@@ -177,31 +199,86 @@ void Miner::flush_pool(uint64_t from) {
     const uint32_t cnt = (uint32_t)(n - from);
     std::vector<uint64_t> lp(cnt + 1);
     for (uint32_t i = 0; i <= cnt; ++i) lp[i] = cptr_[from + i] - cptr_[from];
-    const uint64_t ni = lp[cnt];
-    DevBuf dp, di;
-    dp.reserve((cnt + 1) * 8, h_->stream);
-    di.reserve(std::max<uint64_t>(ni, 1) * 4, h_->stream);
-    SG_CUDA_TRY(cudaMemcpyAsync(dp.ptr, lp.data(), (cnt + 1) * 8, cudaMemcpyHostToDevice, h_->stream));
-    SG_CUDA_TRY(cudaMemcpyAsync(di.ptr, citems_.data() + cptr_[from], ni * 4, cudaMemcpyHostToDevice, h_->stream));
-    launch_pool_append(pool_.as<uint64_t>(), pool_words_, dp.as<uint64_t>(), di.as<uint32_t>(), from, cnt,
-                       h_->stream);
+    const uint64_t *dp = p_ptr_.put(lp.data(), cnt + 1, h_->stream);
+    const uint32_t *di = p_items_.put(citems_.data() + cptr_[from], lp[cnt], h_->stream);
+    launch_pool_append(pool_.as<uint64_t>(), pool_words_, dp, di, from, cnt, h_->stream);
     ++launches_;
-    SG_CUDA_TRY(cudaStreamSynchronize(h_->stream));
-    dp.release();
-    di.release();
     pool_n_ = n;
+}
+
+void Miner::load_cooc() {
+    const uint32_t d = ds_.d;
+    cooc_.assign((size_t)d * d, 0);
+    if (d == 0 || d > 8192) return;
+    DevBuf &out = w_.cooc;
+    out.reserve((size_t)d * d * 4, h_->stream);
+    cooc_device(ds_.bitmaps.as<uint64_t>(), d, ds_.n_words, ds_.stride, out.as<uint32_t>(), 1, h_->stream, h_->n_sm,
+                nullptr, 0, &launches_);
+    SG_CUDA_TRY(cudaMemcpyAsync(cooc_.data(), out.ptr, (size_t)d * d * 4, cudaMemcpyDeviceToHost, h_->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(h_->stream));
+}
+
+// Features of the extension H -> H u {e} (the order of sgfim/mlp.py FEATURES):
+// prefix support, item support, extension support (fractions of n), the
+// conditional density s / sup(H), depth / 16, min and mean over h in H of
+// cooc(e, h) / sup(e), and the sibling position pos / nf.
+void Miner::features(const std::vector<uint32_t> &head, uint32_t head_sup, uint32_t e, uint32_t s, uint32_t pos,
+                     uint32_t nf, float *f) const {
+    const double n = (double)std::max<uint64_t>(ds_.n_txn, 1);
+    const double se = (double)std::max<uint32_t>(ds_.sup[e], 1);
+    double mn = 1.0, mean = 1.0;
+    if (!head.empty() && !cooc_.empty()) {
+        mn = 1.0;
+        double sum = 0;
+        for (uint32_t hh : head) {
+            const double c = cooc_[(size_t)e * ds_.d + hh] / se;
+            mn = std::min(mn, c);
+            sum += c;
+        }
+        mean = sum / head.size();
+    }
+    f[0] = (float)(head_sup / n);
+    f[1] = (float)(ds_.sup[e] / n);
+    f[2] = (float)(s / n);
+    f[3] = (float)((double)s / std::max<uint32_t>(head_sup, 1));
+    f[4] = (float)(head.size() / 16.0);
+    f[5] = (float)mn;
+    f[6] = (float)mean;
+    f[7] = (float)(nf ? (double)pos / nf : 0.0);
+}
+
+void Miner::score(const std::vector<float> &feat, size_t n, std::vector<float> &out) {
+    out.assign(n, 0.f);
+    if (n == 0) return;
+    const Scorer &sc = h_->scorer;
+    cudaStream_t st = h_->stream;
+    const float *X = feat_.put(feat.data(), n * kDim, st);
+    score_.reserve(n * 4, st);
+    hscore_.reserve(n * 4);
+    launch_mlp_forward(X, (uint32_t)n, kDim, sc.hidden, sc.w1.as<uint16_t>(), sc.b1.as<float>(), sc.w2.as<uint16_t>(),
+                       sc.b2.as<float>(), sc.w3.as<uint16_t>(), sc.b3.as<float>(), nullptr, nullptr,
+                       score_.as<float>(), st);
+    ++launches_;
+    SG_CUDA_TRY(cudaMemcpyAsync(hscore_.ptr, score_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(out.data(), hscore_.ptr, n * 4);
 }
 
 int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out) {
     *out = nullptr;
     if (!ds_.loaded) return fail(h_, SGFIM_ESTATE, "no dataset loaded");
     if (p_.min_count < 1) return fail(h_, SGFIM_EINVAL, "min_count must be >= 1");
+    if (p_.order > SGFIM_ORDER_SUPPORT_DESC) return fail(h_, SGFIM_EINVAL, "unknown order");
     if (p_.order == SGFIM_ORDER_LEARNED && !h_->scorer.loaded)
         return fail(h_, SGFIM_ESTATE, "learned order requested but no scorer loaded");
+    if (p_.order == SGFIM_ORDER_LEARNED && h_->scorer.in_dim != kDim)
+        return fail(h_, SGFIM_EINVAL, "scorer input width must equal SGFIM_TRACE_DIM");
     thr_ = p_.min_count;
     t0_ = Clock::now();
     cudaStream_t st = h_->stream;
     const uint32_t d = ds_.d;
+    need_feat_ = p_.order == SGFIM_ORDER_LEARNED || p_.record_trace;
+    if (need_feat_) load_cooc();
 
     // frequent items, ascending support (ties ascending id)
     std::vector<uint32_t> freq;
@@ -212,7 +289,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     // mask arena
     slot_words_ = ds_.stride;
     const uint64_t slot_bytes = slot_words_ * 8;
-    uint64_t budget = h_->hbm_budget / 4;
+    const uint64_t budget = h_->hbm_budget / 4;
     uint64_t max_slots = std::min<uint64_t>(1u << 20, budget / std::max<uint64_t>(slot_bytes, 1));
     max_slots = std::min<uint64_t>(max_slots, std::max<uint64_t>(4096, (uint64_t)freq.size() * 64));
     if (max_slots < 64) max_slots = 64;
@@ -221,20 +298,34 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     for (uint64_t i = 0; i < max_slots; ++i) free_slots_[i] = (uint32_t)(max_slots - 1 - i);
     pool_reserve(65536);
 
-    const uint64_t qmax = 1u << 17;                         // queries per wave
+    const uint64_t qmax = 1u << 17;                                // queries per wave
     const uint64_t nmax = h_->wave_nodes ? h_->wave_nodes : 8192;  // nodes per wave
     std::vector<MNode> stack;
-    {
+    if (!freq.empty()) {
         MNode root;
         root.tail = freq;
         root.sup = (uint32_t)ds_.n_txn;
-        if (!freq.empty()) stack.push_back(std::move(root));
+        root.id = 0;
+        parent_.push_back(kNoNode);
+        stack.push_back(std::move(root));
     }
     uint32_t next_ck = 0;
     std::vector<MNode> wave;
     QuerySet qs, qpool, qfhut, qchild;
-    std::vector<uint32_t> counts, pool_hit, fhut_cnt;
+    std::vector<uint32_t> counts, pool_hit, fhut_cnt, tmp;
+    std::vector<float> wfeat, wscore;
     int status = SGFIM_OK;
+
+    struct Work {
+        std::vector<uint32_t> head;                    // after PEP
+        std::vector<std::pair<uint32_t, uint32_t>> f;  // (support, item), ascending
+        int kind = 0;                                  // 0 leaf, 1 internal
+        size_t pool_q = 0, fhut_q = 0;
+        size_t kid0 = 0, nkids = 0;                    // range in the wave's kid list
+    };
+    std::vector<Work> work;
+    std::vector<MNode> kids;
+    std::vector<uint32_t> child_parent, child_slot;
 
     while (!stack.empty()) {
         // ---- pop a wave
@@ -251,7 +342,6 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         nodes_ += wave.size();
         // ---- phase A: s_e for every tail item
         qs.clear();
-        std::vector<uint32_t> tmp;
         for (const MNode &nd : wave) {
             for (uint32_t e : nd.tail) {
                 if (nd.slot != kNoSlot) {
@@ -265,13 +355,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts);
         // ---- phase B: PEP, ordering, pool and FHUT queries
-        struct Work {
-            std::vector<uint32_t> head;           // after PEP
-            std::vector<std::pair<uint32_t, uint32_t>> f;  // (support, item) ascending
-            int kind = 0;                         // 0 leaf, 1 internal
-            size_t pool_q = 0, fhut_q = 0;
-        };
-        std::vector<Work> work(wave.size());
+        work.assign(wave.size(), Work{});
         qpool.clear();
         qfhut.clear();
         size_t off = 0;
@@ -286,26 +370,18 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 else wk.f.emplace_back(s, nd.tail[j]);
             }
             off += nd.tail.size();
-            std::stable_sort(wk.f.begin(), wk.f.end(),
-                             [](const std::pair<uint32_t, uint32_t> &a, const std::pair<uint32_t, uint32_t> &b) {
-                                 return a.first < b.first || (a.first == b.first && a.second < b.second);
-                             });
+            std::sort(wk.f.begin(), wk.f.end());
+            tmp.assign(wk.head.begin(), wk.head.end());
+            for (auto &pr : wk.f) tmp.push_back(pr.second);
+            wk.pool_q = qpool.size();
+            qpool.add(tmp.data(), tmp.size(), kNoSlot);
             if (wk.f.empty()) {
                 wk.kind = 0;
-                wk.pool_q = qpool.size();
-                qpool.add(wk.head.data(), wk.head.size(), kNoSlot);
             } else {
                 wk.kind = 1;
-                tmp.assign(wk.head.begin(), wk.head.end());
-                for (auto &pr : wk.f) tmp.push_back(pr.second);
-                wk.pool_q = qpool.size();
-                qpool.add(tmp.data(), tmp.size(), kNoSlot);
                 wk.fhut_q = qfhut.size();
-                if (nd.slot != kNoSlot) {
-                    qfhut.add(tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
-                } else {
-                    qfhut.add(tmp.data(), tmp.size(), kNoSlot);
-                }
+                if (nd.slot != kNoSlot) qfhut.add(tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
+                else qfhut.add(tmp.data(), tmp.size(), kNoSlot);
             }
         }
         if (pool_n_ > 0) {
@@ -315,112 +391,133 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             pool_hit.assign(qpool.size(), 0);
         }
         run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt);
-        // ---- phase C: emit candidates, expand children
+        // ---- phase C: emit candidates, create children
         const uint64_t pool_before = csup_.size();
         qchild.clear();
-        std::vector<uint32_t> child_parent, child_slot;
-        std::vector<MNode> children_rev;
+        child_slot.clear();
+        kids.clear();
+        wfeat.clear();
         for (size_t i = 0; i < wave.size(); ++i) {
             MNode &nd = wave[i];
             Work &wk = work[i];
             if (wk.kind == 0) {
-                if (!wk.head.empty() && pool_hit[wk.pool_q] == 0) emit(wk.head, nd.sup);
+                if (!wk.head.empty() && pool_hit[wk.pool_q] == 0) emit(wk.head, nd.sup, nd.id);
                 continue;
             }
             if (pool_hit[wk.pool_q] != 0) continue;  // HUT
             if (fhut_cnt[wk.fhut_q] >= thr_) {       // FHUT
                 tmp.assign(wk.head.begin(), wk.head.end());
                 for (auto &pr : wk.f) tmp.push_back(pr.second);
-                emit(tmp, fhut_cnt[wk.fhut_q]);
+                emit(tmp, fhut_cnt[wk.fhut_q], nd.id);
                 continue;
             }
-            // children in search order; pushed in reverse so the first is popped first
             const size_t nf = wk.f.size();
-            std::vector<MNode> kids(nf);
+            wk.kid0 = kids.size();
+            wk.nkids = nf;
             for (size_t j = 0; j < nf; ++j) {
-                MNode &c = kids[j];
+                MNode c;
                 c.head = wk.head;
                 c.head.push_back(wk.f[j].second);
                 c.sup = wk.f[j].first;
                 c.tail.reserve(nf - j - 1);
                 for (size_t k = j + 1; k < nf; ++k) c.tail.push_back(wk.f[k].second);
-                if (c.tail.empty()) {
-                    // a child without tail is a leaf: its own wave will test it against the pool
-                    c.slot = kNoSlot;
-                    continue;
-                }
-                c.slot = alloc_slot();
-                if (c.slot != kNoSlot) {
-                    if (nd.slot != kNoSlot) {
-                        const uint32_t e = wk.f[j].second;
-                        qchild.add(&e, 1, nd.slot);
-                    } else {
-                        qchild.add(c.head.data(), c.head.size(), kNoSlot);
+                c.id = (uint32_t)parent_.size();
+                parent_.push_back(nd.id);
+                if (need_feat_) {
+                    float f[kDim];
+                    features(wk.head, nd.sup, wk.f[j].second, wk.f[j].first, (uint32_t)j, (uint32_t)nf, f);
+                    wfeat.insert(wfeat.end(), f, f + kDim);
+                    if (p_.record_trace) {
+                        tfeat_.insert(tfeat_.end(), f, f + kDim);
+                        tnode_.push_back(c.id);
                     }
-                    child_slot.push_back(c.slot);
                 }
+                if (!c.tail.empty()) {
+                    // a child without tail is a leaf: its own wave tests it against the pool
+                    c.slot = alloc_slot();
+                    if (c.slot != kNoSlot) {
+                        if (nd.slot != kNoSlot) {
+                            const uint32_t e = wk.f[j].second;
+                            qchild.add(&e, 1, nd.slot);
+                        } else {
+                            qchild.add(c.head.data(), c.head.size(), kNoSlot);
+                        }
+                        child_slot.push_back(c.slot);
+                    }
+                }
+                kids.push_back(std::move(c));
             }
-            for (size_t j = nf; j-- > 0;) children_rev.push_back(std::move(kids[j]));
         }
         // child masks: mask(child) = mask(parent) & AND rows(list)
         if (qchild.size()) {
-            dq_ptr_.reserve((qchild.size() + 1) * 8, st);
-            // reuse the generic staging: child masks use the query arrays + a slot list
             const size_t n = qchild.size();
-            std::vector<uint32_t> pslot(qchild.slot);
-            DevBuf dptr, ditems, dps, dcs;
-            dptr.reserve((n + 1) * 8, st);
-            ditems.reserve(std::max<size_t>(qchild.items.size(), 1) * 4, st);
-            dps.reserve(n * 4, st);
-            dcs.reserve(n * 4, st);
-            SG_CUDA_TRY(cudaMemcpyAsync(dptr.ptr, qchild.ptr.data(), (n + 1) * 8, cudaMemcpyHostToDevice, st));
-            SG_CUDA_TRY(cudaMemcpyAsync(ditems.ptr, qchild.items.data(), qchild.items.size() * 4,
-                                        cudaMemcpyHostToDevice, st));
-            SG_CUDA_TRY(cudaMemcpyAsync(dps.ptr, pslot.data(), n * 4, cudaMemcpyHostToDevice, st));
-            SG_CUDA_TRY(cudaMemcpyAsync(dcs.ptr, child_slot.data(), n * 4, cudaMemcpyHostToDevice, st));
-            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(), ds_.stride,
-                               dptr.as<uint64_t>(), ditems.as<uint32_t>(), dps.as<uint32_t>(), dcs.as<uint32_t>(),
-                               (uint32_t)n, st, h_->n_sm);
+            const uint64_t *dptr = c_ptr_.put(qchild.ptr.data(), n + 1, st);
+            const uint32_t *ditems = c_items_.put(qchild.items.data(), qchild.items.size(), st);
+            const uint32_t *dps = c_ps_.put(qchild.slot.data(), n, st);
+            const uint32_t *dcs = c_cs_.put(child_slot.data(), n, st);
+            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(),
+                               ds_.stride, dptr, ditems, dps, dcs, (uint32_t)n, st, h_->n_sm);
             ++launches_;
-            SG_CUDA_TRY(cudaStreamSynchronize(st));
-            dptr.release(); ditems.release(); dps.release(); dcs.release();
         }
-        // parents' masks are no longer needed
+        // sibling visiting order
+        if (p_.order == SGFIM_ORDER_LEARNED) score(wfeat, kids.size(), wscore);
+        for (size_t i = wave.size(); i-- > 0;) {
+            // stack is LIFO: nodes pushed later are popped first; keep wave order
+            Work &wk = work[i];
+            if (wk.kind == 0 || wk.nkids == 0) continue;
+            std::vector<size_t> ord(wk.nkids);
+            std::iota(ord.begin(), ord.end(), wk.kid0);
+            if (p_.order == SGFIM_ORDER_SUPPORT_DESC) {
+                std::reverse(ord.begin(), ord.end());
+            } else if (p_.order == SGFIM_ORDER_LEARNED) {
+                std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return wscore[a] > wscore[b]; });
+            }
+            for (size_t j = ord.size(); j-- > 0;) stack.push_back(std::move(kids[ord[j]]));
+        }
+        // parents' masks are no longer needed once the child-mask kernel ran (stream order)
         for (MNode &nd : wave)
             if (nd.slot != kNoSlot) free_slots_.push_back(nd.slot);
-        for (MNode &c : children_rev) stack.push_back(std::move(c));
         flush_pool(pool_before);
         // ---- checkpoints, limits
         const double el = elapsed();
         while (next_ck < n_ckpt && el >= ckpts[next_ck]) {
             if (cb) {
-                std::vector<uint64_t> op(cptr_);
                 std::vector<uint32_t> oi(citems_.size());
                 for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
                 sgfim_checkpoint ck;
                 ck.t_s = ckpts[next_ck];
                 ck.elapsed_s = el;
                 ck.n_emitted = csup_.size();
-                ck.set_ptr = op.data();
+                ck.set_ptr = cptr_.data();
                 ck.items = oi.data();
                 ck.support = csup_.data();
                 ck.nodes = nodes_;
-                if (cb(user, &ck) != 0) { status = SGFIM_ECANCELED; break; }
+                if (cb(user, &ck) != 0) {
+                    status = SGFIM_ECANCELED;
+                    break;
+                }
             }
             ++next_ck;
         }
         if (status != SGFIM_OK) break;
-        if (p_.time_limit_s > 0 && el > p_.time_limit_s) { status = SGFIM_ETIMEDOUT; break; }
-        if (p_.node_limit && nodes_ > p_.node_limit) { status = SGFIM_ENOMEM; break; }
+        if (p_.time_limit_s > 0 && el > p_.time_limit_s) {
+            status = SGFIM_ETIMEDOUT;
+            break;
+        }
+        if (p_.node_limit && nodes_ > p_.node_limit) {
+            status = SGFIM_ENOMEM;
+            break;
+        }
     }
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
     if (status != SGFIM_OK) {
         h_->launches += launches_;
-        return fail(h_, status, status == SGFIM_ECANCELED ? "stopped by checkpoint callback"
+        return fail(h_, status, status == SGFIM_ECANCELED    ? "stopped by checkpoint callback"
                                 : status == SGFIM_ETIMEDOUT ? "time limit expired"
                                                             : "node limit exceeded");
     }
     // remaining checkpoints fire once the search is complete
-    if (cb) {
+    if (cb && next_ck < n_ckpt) {
         const double el = elapsed();
         std::vector<uint32_t> oi(citems_.size());
         for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
@@ -444,7 +541,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
 int Miner::finish(sgfim_result **out) {
     const uint64_t n = csup_.size();
     // maximality filter: members of the pool containing each candidate
-    std::vector<uint32_t> keep(n, 1);
+    std::vector<uint8_t> keep(n, 1);
     if (n > 1) {
         const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
         const uint64_t chunk = 1u << 20;
@@ -456,6 +553,15 @@ int Miner::finish(sgfim_result **out) {
             for (uint64_t c = a; c < b; ++c) qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
             run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_COUNT, cnt);
             for (uint64_t c = a; c < b; ++c) keep[c] = cnt[c - a] <= 1;
+        }
+    }
+    // trace labels: every ancestor of a node that emitted a final MFI
+    std::vector<uint8_t> pos;
+    if (p_.record_trace) {
+        pos.assign(parent_.size(), 0);
+        for (uint64_t c = 0; c < n; ++c) {
+            if (!keep[c]) continue;
+            for (uint32_t v = cnode_[c]; v != kNoNode && !pos[v]; v = parent_[v]) pos[v] = 1;
         }
     }
     // root rule: the highest original id of the set must be a root
@@ -495,18 +601,27 @@ int Miner::finish(sgfim_result **out) {
     r->items = static_cast<uint32_t *>(malloc(std::max<uint64_t>(total, 1) * 4));
     r->support = static_cast<uint32_t *>(malloc(std::max<uint64_t>(m, 1) * 4));
     r->emit_time_s = static_cast<double *>(malloc(std::max<uint64_t>(m, 1) * 8));
-    if (!r->set_ptr || !r->items || !r->support || !r->emit_time_s) {
+    const uint64_t tn = p_.record_trace ? tnode_.size() : 0;
+    r->trace_n = tn;
+    r->trace_dim = kDim;
+    r->trace_features = static_cast<float *>(malloc(std::max<uint64_t>(tn * kDim, 1) * 4));
+    r->trace_labels = static_cast<uint8_t *>(malloc(std::max<uint64_t>(tn, 1)));
+    if (!r->set_ptr || !r->items || !r->support || !r->emit_time_s || !r->trace_features || !r->trace_labels) {
         sgfim_result_free(r);
         return fail(h_, SGFIM_ENOMEM, "result allocation failed");
     }
     r->set_ptr[0] = 0;
-    uint64_t pos = 0;
+    uint64_t at = 0;
     for (uint64_t i = 0; i < m; ++i) {
         const uint64_t c = order[i];
-        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[pos++] = ds_.d2o[citems_[k]];
-        r->set_ptr[i + 1] = pos;
+        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[at++] = ds_.d2o[citems_[k]];
+        r->set_ptr[i + 1] = at;
         r->support[i] = csup_[c];
         r->emit_time_s[i] = ctime_[c];
+    }
+    if (tn) {
+        memcpy(r->trace_features, tfeat_.data(), tn * kDim * 4);
+        for (uint64_t t = 0; t < tn; ++t) r->trace_labels[t] = pos[tnode_[t]];
     }
     r->n_txn = ds_.n_txn;
     r->min_count = thr_;
@@ -529,15 +644,15 @@ int mine_impl(sgfim_handle *h, const sgfim_mine_params *p, const double *ckpts, 
     if (!h->ds.loaded) return fail(h, SGFIM_ESTATE, "no dataset loaded");
     if (h->ds.n_txn == 0 || h->ds.d == 0) {
         // nothing to mine: an empty, valid result
-        Miner m(h, *p);
-        sgfim_mine_params q = *p;
-        (void)q;
         sgfim_result *r = static_cast<sgfim_result *>(calloc(1, sizeof(sgfim_result)));
         if (!r) return fail(h, SGFIM_ENOMEM, "result allocation failed");
         r->set_ptr = static_cast<uint64_t *>(calloc(1, 8));
         r->items = static_cast<uint32_t *>(calloc(1, 4));
         r->support = static_cast<uint32_t *>(calloc(1, 4));
         r->emit_time_s = static_cast<double *>(calloc(1, 8));
+        r->trace_features = static_cast<float *>(calloc(1, 4));
+        r->trace_labels = static_cast<uint8_t *>(calloc(1, 1));
+        r->trace_dim = kDim;
         r->n_txn = h->ds.n_txn;
         r->min_count = p->min_count;
         *out = r;

@@ -11,7 +11,7 @@
 // allocated by the call.
 //
 // Costs of that choice: every GPU on which the library is loaded keeps the
-// array (kNoAllocScratchBytes, about 21 MB) until the process exits; inputs
+// array (kNoAllocScratchBytes, about 25 MB) until the process exits; inputs
 // larger than SGFIM_NOALLOC_MAX_CAND candidates are rejected; and all calls
 // share the one array, so calls that overlap on the GPU race.
 #include <mutex>
@@ -23,9 +23,8 @@
 namespace {
 
 constexpr uint64_t kMaxCand = SGFIM_NOALLOC_MAX_CAND;
-constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
-// Same layout as sg::support_scratch_bytes(): records, overflow list, counter.
-constexpr size_t kNoAllocScratchBytes = align256(kMaxCand * 16) + align256(kMaxCand * 4) + 256;
+// The support kernels' scratch layout for the largest accepted input.
+constexpr size_t kNoAllocScratchBytes = sg::support_scratch_bytes_for(kMaxCand);
 
 __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
 __device__ __align__(256) uint32_t g_dev_err[64];

@@ -22,7 +22,8 @@ OK, EINVAL, ENOMEM, EIO, EDEVICE, ESTATE, ETIMEDOUT, ECANCELED, ENODATA = 0, -1,
 ECAPACITY = -9
 NOALLOC_MAX_CAND = 1048576
 ROOTS_ALL, ROOTS_LIST, ROOTS_MINCOUNT = 0, 1, 2
-ORDER_SUPPORT, ORDER_LEARNED = 0, 1
+ORDER_SUPPORT, ORDER_LEARNED, ORDER_SUPPORT_DESC = 0, 1, 2
+TRACE_DIM = 8
 COOC_AUTO, COOC_POPC, COOC_BMMA, COOC_TC_F8 = 0, 1, 2, 3
 
 
@@ -42,13 +43,15 @@ class Result(C.Structure):
     _fields_ = [("n_sets", C.c_uint64), ("set_ptr", u64p), ("items", u32p), ("support", u32p),
                 ("emit_time_s", f64p), ("n_txn", C.c_uint64), ("min_count", C.c_uint32),
                 ("elapsed_s", C.c_double), ("preprocess_s", C.c_double), ("nodes", C.c_uint64),
-                ("waves", C.c_uint64), ("kernel_launches", C.c_uint64), ("candidates", C.c_uint64)]
+                ("waves", C.c_uint64), ("kernel_launches", C.c_uint64), ("candidates", C.c_uint64),
+                ("trace_n", C.c_uint64), ("trace_dim", C.c_uint32), ("trace_features", f32p),
+                ("trace_labels", C.POINTER(C.c_uint8))]
 
 
 class MineParams(C.Structure):
     _fields_ = [("min_count", C.c_uint32), ("root_rule", C.c_uint32), ("roots", u32p),
                 ("n_roots", C.c_uint32), ("root_min_count", C.c_uint32), ("order", C.c_uint32),
-                ("time_limit_s", C.c_double), ("node_limit", C.c_uint64)]
+                ("time_limit_s", C.c_double), ("node_limit", C.c_uint64), ("record_trace", C.c_uint32)]
 
 
 class Checkpoint(C.Structure):
@@ -94,6 +97,13 @@ SIGNATURES = {
     "sgfim_support_batch_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64,
                                              C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_phase_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PhaseStats), C.c_int]),
+    "sgfim_support_plan_set": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32]),
+    "sgfim_ring_open": (C.c_int, [C.c_int, C.c_uint32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "sgfim_ring_close": (None, [C.c_void_p]),
+    "sgfim_ring_head": (C.c_uint64, [C.c_void_p]),
+    "sgfim_ring_capacity": (C.c_uint64, [C.c_void_p]),
+    "sgfim_ring_append": (C.c_int, [C.c_void_p, u64p, u32p, C.c_uint64]),
+    "sgfim_ring_window_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]),
     "sgfim_support_batch_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
                                               C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),

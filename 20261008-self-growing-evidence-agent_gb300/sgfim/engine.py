@@ -45,6 +45,26 @@ class MineResult:
         self.waves = int(r.waves)
         self.kernel_launches = int(r.kernel_launches)
         self.candidates = int(r.candidates)
+        tn, td = int(r.trace_n), int(r.trace_dim)
+        if tn:
+            self.trace_features = np.ctypeslib.as_array(r.trace_features, shape=(tn * td,)).reshape(tn, td).copy()
+            self.trace_labels = np.ctypeslib.as_array(r.trace_labels, shape=(tn,)).copy()
+        else:
+            self.trace_features = np.zeros((0, td or L.TRACE_DIM), np.float32)
+            self.trace_labels = np.zeros(0, np.uint8)
+
+    def coverage_curve(self, emit_times=None):
+        """Sorted emission times of the final MFIs: coverage(t) = fraction emitted by t."""
+        t = np.sort(self.emit_time_s if emit_times is None else emit_times)
+        return t
+
+    def time_to_coverage(self, frac):
+        """Seconds until ``frac`` of the final MFIs had been emitted."""
+        t = np.sort(self.emit_time_s)
+        if len(t) == 0:
+            return 0.0
+        k = max(1, int(math.ceil(frac * len(t))))
+        return float(t[k - 1])
 
     def __len__(self):
         return len(self.support)
@@ -151,6 +171,12 @@ class Engine:
         self._check(self._L.sgfim_support_batch_device(self._h, bm_ptr, d, n_words, row_stride, cand_ptr_ptr,
                                                        cand_items_ptr, n_cand, out_ptr, stream or None))
 
+    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3}
+
+    def set_support_plan(self, kernel="auto", cands_per_cta=0, waves=0):
+        """Choose the support-batch kernel and its CTA sizing (see sgfim_support_plan_set)."""
+        self._check(self._L.sgfim_support_plan_set(self._h, self.KERNELS[kernel], int(cands_per_cta), int(waves)))
+
     def phase_stats(self, reset=True):
         """Summed CUDA-event phase times of support-batch calls (needs phase_timers=True)."""
         s = L.PhaseStats()
@@ -169,8 +195,10 @@ class Engine:
                                                       stream or None))
 
     # ------------------------------------------------------------ mining
+    ORDERS = {"support": L.ORDER_SUPPORT, "learned": L.ORDER_LEARNED, "support_desc": L.ORDER_SUPPORT_DESC}
+
     def _params(self, min_count, roots=None, root_min_count=None, order="support", time_limit_s=0.0,
-                node_limit=0):
+                node_limit=0, record_trace=False):
         p = L.MineParams()
         p.min_count = int(min_count)
         p.root_rule = L.ROOTS_ALL
@@ -187,9 +215,10 @@ class Engine:
         elif root_min_count is not None:
             p.root_rule = L.ROOTS_MINCOUNT
             p.root_min_count = int(root_min_count)
-        p.order = L.ORDER_LEARNED if order == "learned" else L.ORDER_SUPPORT
+        p.order = self.ORDERS[order]
         p.time_limit_s = float(time_limit_s)
         p.node_limit = int(node_limit)
+        p.record_trace = 1 if record_trace else 0
         return p
 
     def mine(self, min_count, **kw):
@@ -204,10 +233,11 @@ class Engine:
         finally:
             self._L.sgfim_result_free(res)
 
-    def mine_anytime(self, min_count, checkpoints, callback=None, **kw):
+    def mine_anytime(self, min_count, checkpoints, callback=None, materialize=True, **kw):
         """Mine with wall-clock checkpoints.  ``callback(t_s, elapsed_s, sets)``
         receives the emitted candidates as a list of (ids tuple, support);
-        returning True stops the search.  Returns (result, records)."""
+        returning True stops the search.  ``materialize=False`` keeps only the
+        counts in the records (no per-set Python objects).  Returns (result, records)."""
         p = self._params(min_count, **kw)
         cks = np.ascontiguousarray(checkpoints, dtype=np.float64)
         records = []
@@ -215,11 +245,13 @@ class Engine:
         def _cb(user, ckp):
             ck = ckp.contents
             n = int(ck.n_emitted)
-            ptr = np.ctypeslib.as_array(ck.set_ptr, shape=(n + 1,)) if n else np.zeros(1, np.uint64)
-            tot = int(ptr[-1])
-            it = np.ctypeslib.as_array(ck.items, shape=(tot,)) if tot else np.zeros(0, np.uint32)
-            sp = np.ctypeslib.as_array(ck.support, shape=(n,)) if n else np.zeros(0, np.uint32)
-            sets = [(tuple(int(x) for x in it[ptr[i]:ptr[i + 1]]), int(sp[i])) for i in range(n)]
+            sets = None
+            if materialize:
+                ptr = np.ctypeslib.as_array(ck.set_ptr, shape=(n + 1,)) if n else np.zeros(1, np.uint64)
+                tot = int(ptr[-1])
+                it = np.ctypeslib.as_array(ck.items, shape=(tot,)) if tot else np.zeros(0, np.uint32)
+                sp = np.ctypeslib.as_array(ck.support, shape=(n,)) if n else np.zeros(0, np.uint32)
+                sets = [(tuple(int(x) for x in it[ptr[i]:ptr[i + 1]]), int(sp[i])) for i in range(n)]
             records.append({"t_s": ck.t_s, "elapsed_s": ck.elapsed_s, "n_emitted": n, "nodes": int(ck.nodes),
                             "sets": sets})
             if callback is not None:

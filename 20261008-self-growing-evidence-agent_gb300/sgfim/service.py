@@ -1,0 +1,340 @@
+"""Sliding-window MFI mining service on one GPU.
+
+Workload "windows-4096": a stream of transactions (21 sensors x 6 bins = 126
+items, one item per sensor per transaction, 8-regime mixture) arrives at
+``stream_rate`` transactions/s and is appended into a device-resident bitmap
+ring (sgfim_ring_*; appends evict the oldest transactions).  Requests arrive
+as a Poisson process; request i asks for the MFIs of the newest L_i
+transactions at its arrival, L_i log-uniform in [512, 65,536], at floor
+ceil(2% * L_i).  Worker threads, each owning an engine handle (its own CUDA
+stream and reused device workspace), take requests in arrival order; a request
+is admitted when its device-memory estimate fits the service's HBM budget.
+Latency = completion - arrival.  Reports p50/p99 latency and windows/s.
+
+The reference has no service (it transactionises windows on the host,
+code/pipeline/skab_spike.py:61-80, and starts one engine process per file).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import heapq
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from . import datagen
+from .engine import Engine, SgfimError
+
+WORKLOAD = dict(n_req=4096, len_lo=512, len_hi=65536, n_sensors=21, n_bins=6, n_regimes=8, alpha_bin=0.3,
+                floor_frac=0.02, rate_hz=2000.0, stream_rate=100_000.0, ring_txn=1 << 17)
+
+
+class Ring:
+    """Python handle of sgfim_ring (device-resident transaction ring)."""
+
+    def __init__(self, n_items, capacity_txn, device=0):
+        self._L = L.load()
+        r = C.c_void_p()
+        rc = self._L.sgfim_ring_open(device, n_items, capacity_txn, C.byref(r))
+        if rc != 0:
+            raise SgfimError(rc, "sgfim_ring_open failed")
+        self._r = r
+
+    @property
+    def head(self):
+        return int(self._L.sgfim_ring_head(self._r))
+
+    @property
+    def capacity(self):
+        return int(self._L.sgfim_ring_capacity(self._r))
+
+    def append(self, row_ptr, items):
+        row_ptr = np.ascontiguousarray(row_ptr, np.uint64)
+        items = np.ascontiguousarray(items, np.uint32)
+        if len(items) == 0:
+            items = np.zeros(1, np.uint32)
+        rc = self._L.sgfim_ring_append(self._r, row_ptr.ctypes.data_as(L.u64p), items.ctypes.data_as(L.u32p),
+                                       len(row_ptr) - 1)
+        if rc != 0:
+            raise SgfimError(rc, "sgfim_ring_append failed")
+
+    def window_load(self, eng, start, length):
+        rc = self._L.sgfim_ring_window_load(self._r, eng.handle, int(start), int(length))
+        eng._check(rc)
+
+    def close(self):
+        if getattr(self, "_r", None):
+            self._L.sgfim_ring_close(self._r)
+            self._r = None
+
+
+@dataclass(order=True)
+class Request:
+    arrival: float
+    idx: int = field(compare=False)
+    length: int = field(compare=False)
+    end: int = field(compare=False, default=0)       # stream position of the window end
+    start_s: float = field(compare=False, default=0.0)
+    done_s: float = field(compare=False, default=0.0)
+    n_mfis: int = field(compare=False, default=0)
+    error: str = field(compare=False, default="")
+    result: object = field(compare=False, default=None)
+
+
+def make_requests(n, rate_hz, len_lo, len_hi, seed):
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_hz, n)
+    arrival = np.cumsum(gaps)
+    lengths = np.exp(rng.uniform(np.log(len_lo), np.log(len_hi), n)).astype(np.int64)
+    return [Request(float(a), i, int(L_)) for i, (a, L_) in enumerate(zip(arrival, lengths))]
+
+
+def window_bytes(length, n_items=126):
+    """Device-memory estimate of one window's mining: bitmap + mask arena + pool."""
+    words = ((length + 63) // 64 + 1) & ~1
+    slots = max(4096, n_items * 64)          # the miner's mask-arena sizing
+    return (n_items + slots) * words * 8 + n_items * 1026 * 8
+
+
+class WindowService:
+    def __init__(self, workers=8, hbm_budget=8 << 30, device=0, ring_txn=WORKLOAD["ring_txn"], n_items=126,
+                 keep_results=False):
+        self.ring = Ring(n_items, ring_txn, device)
+        self.engines = [Engine(device=device) for _ in range(workers)]
+        self.budget = hbm_budget
+        self.n_items = n_items
+        self.keep = keep_results
+        self._cv = threading.Condition()
+        self._in_use = 0
+        self._queue = []
+        self._closed = False
+
+    def close(self):
+        for e in self.engines:
+            e.close()
+        self.ring.close()
+
+    # ------------------------------------------------------------ admission
+    def _admit(self, need):
+        with self._cv:
+            while self._in_use + need > self.budget and self._in_use > 0:
+                self._cv.wait()
+            self._in_use += need
+
+    def _release(self, need):
+        with self._cv:
+            self._in_use -= need
+            self._cv.notify_all()
+
+    # ------------------------------------------------------------ run
+    def run(self, stream_rows, requests, stream_rate, floor_frac, warm_txn=None):
+        """Replay the stream and the requests in real time; returns the report."""
+        rp_all, it_all = datagen.txns_to_csr(stream_rows)
+        total = len(rp_all) - 1
+        warm = warm_txn if warm_txn is not None else WORKLOAD["len_hi"]
+        self.ring.append(rp_all[:warm + 1], it_all[:int(rp_all[warm])])
+        appended = warm
+        t0 = time.perf_counter()
+        lock = threading.Lock()
+        work = []          # heap of admitted-to-queue requests by arrival
+        done = []
+        stop = threading.Event()
+
+        def produce_until(pos):
+            nonlocal appended
+            with lock:
+                if pos > appended:
+                    a, b = appended, min(pos, total)
+                    if b > a:
+                        self.ring.append(rp_all[a:b + 1] - rp_all[a], it_all[int(rp_all[a]):int(rp_all[b])])
+                        appended = b
+
+        def stream_pos(t):
+            return min(total, warm + int(stream_rate * t))
+
+        def dispatcher():
+            for rq in requests:
+                now = time.perf_counter() - t0
+                if rq.arrival > now:
+                    time.sleep(rq.arrival - now)
+                rq.end = stream_pos(rq.arrival)
+                produce_until(rq.end)
+                with self._cv:
+                    heapq.heappush(work, rq)
+                    self._cv.notify_all()
+            stop.set()
+            with self._cv:
+                self._cv.notify_all()
+
+        def worker(eng):
+            while True:
+                with self._cv:
+                    while not work and not stop.is_set():
+                        self._cv.wait()
+                    if not work:
+                        return
+                    rq = heapq.heappop(work)
+                need = window_bytes(rq.length, self.n_items)
+                self._admit(need)
+                try:
+                    rq.start_s = time.perf_counter() - t0
+                    length = min(rq.length, rq.end)
+                    self.ring.window_load(eng, rq.end - length, length)
+                    thr = max(1, int(np.ceil(floor_frac * length)))
+                    res = eng.mine(thr)
+                    rq.n_mfis = len(res)
+                    if self.keep:
+                        rq.result = res.as_dict()
+                except SgfimError as e:
+                    rq.error = str(e)
+                finally:
+                    self._release(need)
+                rq.done_s = time.perf_counter() - t0
+                with lock:
+                    done.append(rq)
+
+        threads = [threading.Thread(target=worker, args=(e,), daemon=True) for e in self.engines]
+        for t in threads:
+            t.start()
+        disp = threading.Thread(target=dispatcher, daemon=True)
+        disp.start()
+        disp.join()
+        for t in threads:
+            t.join()
+        wall = time.perf_counter() - t0
+        lat = np.array([r.done_s - r.arrival for r in done])
+        errors = [r for r in done if r.error]
+        first, last = min(r.arrival for r in requests), max(r.done_s for r in done)
+        return {"windows": len(done), "errors": len(errors), "wall_s": wall,
+                "windows_per_s": len(done) / max(last - first, 1e-9),
+                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3), "max_ms": float(lat.max() * 1e3),
+                "mfis_total": int(sum(r.n_mfis for r in done)), "requests": done}
+
+
+def stream_rows_for(n_req=WORKLOAD["n_req"], rate_hz=WORKLOAD["rate_hz"], stream_rate=WORKLOAD["stream_rate"],
+                    seed=0):
+    duration = n_req / rate_hz * 1.5 + 1.0
+    n = WORKLOAD["len_hi"] + int(stream_rate * duration)
+    return datagen.regime_txns(n, WORKLOAD["n_sensors"], WORKLOAD["n_bins"], WORKLOAD["n_regimes"],
+                               WORKLOAD["alpha_bin"], seed=seed)
+
+
+# ---------------------------------------------------------------- exactness / CPU arm (oracle, spawn pool)
+_ROWS = None
+
+
+def _pool_init(rows):
+    global _ROWS
+    _ROWS = rows
+
+
+def _check_window(args):
+    """Oracle MFIs of one window (runs in a worker process)."""
+    import oracle
+    end, length, thr = args
+    rows = _ROWS[end - length:end]
+    rp, it = datagen.txns_to_csr(rows)
+    bm, _ = oracle.build_bitmaps(rp, it, 126)
+    res, _ = oracle.mine_fast(bm, length, thr)
+    return sorted((tuple(s), c) for s, c in res)
+
+
+def _cpu_window(args):
+    """The reference's miner restated (mine_mfi with its 200,000-node cap) on one window."""
+    import oracle
+    end, length, thr = args
+    rows = _ROWS[end - length:end]
+    rp, it = datagen.txns_to_csr(rows)
+    bm, _ = oracle.build_bitmaps(rp, it, 126)
+    t = time.perf_counter()
+    try:
+        oracle.mine_mfi(bm, length, min_count=thr, node_cap=200_000)
+        ok = True
+    except RuntimeError:
+        ok = False
+    return ok, time.perf_counter() - t
+
+
+def main(argv=None):
+    import argparse
+    import json
+    import multiprocessing as mp
+    import os
+    ap = argparse.ArgumentParser(description="sliding-window MFI service, workload windows-4096")
+    ap.add_argument("--requests", type=int, default=WORKLOAD["n_req"])
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
+    ap.add_argument("--check", action="store_true", help="compare every window with the oracle")
+    ap.add_argument("--check-budget-s", type=float, default=240.0)
+    ap.add_argument("--cpu-budget-s", type=float, default=30.0)
+    ap.add_argument("--out", default="")
+    a = ap.parse_args(argv)
+    rows = stream_rows_for(a.requests)
+    reqs = make_requests(a.requests, WORKLOAD["rate_hz"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
+    svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
+                        keep_results=a.check)
+    # warm-up pass on a handful of requests (first-use allocations of every worker)
+    warm = make_requests(2 * a.workers, 4000.0, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=99)
+    svc.run(rows, warm, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
+    svc.ring.close()
+    svc.ring = Ring(126, WORKLOAD["ring_txn"])
+    rep = svc.run(rows, reqs, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
+    svc.close()
+    done = rep.pop("requests")
+    errs = {}
+    for rq in done:
+        if rq.error:
+            errs[rq.error] = errs.get(rq.error, 0) + 1
+    report = {"workload": "windows-4096", "requests": a.requests, "workers": a.workers,
+              "hbm_budget_gb": a.hbm_budget_gb, **rep, "error_kinds": errs,
+              "config": {k: WORKLOAD[k] for k in WORKLOAD}}
+    ctx = mp.get_context("spawn")
+    procs = os.cpu_count() or 1
+    jobs = []
+    for rq in done:
+        length = min(rq.length, rq.end)
+        jobs.append((rq.end, length, max(1, int(np.ceil(WORKLOAD["floor_frac"] * length)))))
+    if a.check:
+        t0 = time.perf_counter()
+        checked = mism = 0
+        with ctx.Pool(procs, initializer=_pool_init, initargs=(rows,)) as pool:
+            for rq, ref in zip(done, pool.imap(_check_window, jobs, chunksize=4)):
+                if rq.result is None:   # the request failed; counted in "errors"
+                    continue
+                got = sorted((tuple(sorted(s)), c) for s, c in rq.result.items())
+                checked += 1
+                mism += got != ref
+                if time.perf_counter() - t0 > a.check_budget_s:
+                    pool.terminate()
+                    break
+        report["exact"] = {"checked": checked, "mismatches": mism}
+    if a.cpu_budget_s > 0:
+        t0 = time.perf_counter()
+        n_ok = n_cap = 0
+        cpu_t = 0.0
+        with ctx.Pool(procs, initializer=_pool_init, initargs=(rows,)) as pool:
+            for ok, dt in pool.imap(_cpu_window, jobs, chunksize=1):
+                n_ok += ok
+                n_cap += not ok
+                cpu_t += dt
+                if time.perf_counter() - t0 > a.cpu_budget_s:
+                    pool.terminate()
+                    break
+        wall = time.perf_counter() - t0
+        report["cpu_baseline"] = {"windows": n_ok + n_cap, "completed": n_ok, "node_cap_hit": n_cap,
+                                  "windows_per_s": (n_ok + n_cap) / wall, "cores": procs, "kind": "port",
+                                  "sample": f"first {n_ok + n_cap} windows in arrival order within "
+                                            f"{a.cpu_budget_s:.0f} s, mine_mfi restated with its 200,000-node cap"}
+    print(json.dumps(report))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(report, f, indent=1)
+    return report
+
+
+if __name__ == "__main__":
+    main()

@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--n-cand", type=int, default=WORKLOAD["n_cand"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cooc", action="store_true")
+    ap.add_argument("--kernel", choices=["auto", "sorted", "staged", "stream"], default="auto")
     return ap.parse_args()
 
 
@@ -74,9 +76,10 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the counting kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k1_staged_support-1m.json")
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of the counting kernel from the committed ncu summary
+    (a one-pass capture of this workload: dram__bytes_read.sum + dram__bytes_write.sum)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_support-1m.json")
     if os.path.exists(path):
         with open(path) as f:
             return json.load(f)
@@ -211,6 +214,7 @@ def main():
     n_cand = len(cp) - 1
     d, w = bm.shape
     eng = Engine(device=local, phase_timers=True)
+    eng.set_support_plan(args.kernel)
     t_bm = torch.from_numpy(bm.view(np.int64)).to(dev)
     t_cp = torch.from_numpy(cp.view(np.int64)).to(dev)
     t_ci = torch.from_numpy(ci.view(np.int32)).to(dev)
@@ -257,12 +261,13 @@ def main():
     count_ms = ps["count_ms"] / max(1, ps["calls"])
     peaks, peak_src = measured_peaks()
     achieved = alg_bytes / (count_ms / 1000.0) / 1e9
-    tr = ncu_traffic()
+    kname = {"auto": "k1_sorted_kernel", "sorted": "k1_sorted_kernel", "staged": "k1_staged_kernel",
+             "stream": "query_kernel"}[args.kernel]
+    tr = ncu_traffic(kname.replace("_kernel", ""))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_source": peak_src,
                 "traffic": (tr["dram_bytes_per_launch"] if tr else None),
-                "kernel": "k1_staged_kernel", "kernel_ms": count_ms,
-                "alg_bytes_per_launch": alg_bytes}
+                "kernel": kname, "kernel_ms": count_ms, "alg_bytes_per_launch": alg_bytes}
 
     # end to end through the host C ABI with pinned buffers
     e2e = None
@@ -288,6 +293,28 @@ def main():
                "d2h_bytes_per_step": int(4 * n_cand), "ms_per_step": e_ms,
                "note": "sgfim_load_bitmaps + sgfim_support_batch per step, pinned host buffers"}
 
+    # the 1,024 x 1,024 co-occurrence matrix of the same bitmaps (both kernel kinds)
+    cooc = {}
+    if not args.no_cooc:
+        t_co = {k: torch.zeros(d * d, dtype=torch.int32, device=dev) for k in (1, 2, 3)}
+        for kind, name in ((1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3")):
+            for _ in range(2):
+                eng.cooccurrence_device(t_bm.data_ptr(), d, w, w, t_co[kind].data_ptr(), kind, stream.cuda_stream)
+            times = []
+            for _ in range(5):
+                flush.fill_(1)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                eng.cooccurrence_device(t_bm.data_ptr(), d, w, w, t_co[kind].data_ptr(), kind, stream.cuda_stream)
+                b.record(stream)
+                torch.cuda.synchronize()
+                times.append(a.elapsed_time(b))
+            ms_c = statistics.median(times)
+            bitops = float(d) * d * WORKLOAD["n_txn"]
+            cooc[name] = {"ms": ms_c, "tbitops": bitops / (ms_c / 1000.0) / 1e12}
+        cooc["kinds_agree"] = bool(torch.equal(t_co[1], t_co[2]) and torch.equal(t_co[1], t_co[3]))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, sup_cpu, n_s = cpu_baseline(bm, cp, ci)
@@ -301,7 +328,7 @@ def main():
                            "candidates_per_gpu": n_cand, "k": "3..8", "bitmap_bytes": int(bm.nbytes),
                            "l2": "flushed (512 MiB write) before every step",
                            "parallelism": f"candidate shards x{world}, no collective on the data path"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "cooccurrence_1024": cooc,
                 "gpu_launches": int(ps["launches"]), "clocks": clk.summary(),
                 "wall_s_timed": wall}
         print(json.dumps(line), flush=True)

@@ -135,13 +135,25 @@ int sgfim_support_batch_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_
  * the item bitmaps. */
 int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
 
+/* Kernel plan of the support-batch entry points (the tuning knobs; the
+ * reference tunes its wave engine with environment variables instead,
+ * BMMA_WAVE_CAP / BMMA_SPLITK_OFF / BMMA_MASK_WPB, kernel_bmma.cu:351-368).
+ * kernel: SGFIM_KERNEL_*; cands_per_cta: candidates a CTA owns (0 = derived);
+ * waves: CTAs per SM over the grid when cands_per_cta is 0 (0 = the kernel's
+ * default: 1 for SORTED, 2 for STAGED). */
+#define SGFIM_KERNEL_AUTO 0    /* staged when it fits shared memory, else streaming */
+#define SGFIM_KERNEL_STAGED 1  /* TMA-staged chunks, candidates in input order */
+#define SGFIM_KERNEL_SORTED 2  /* TMA-staged chunks, candidates sorted by (k, first item); ids < 1024 */
+#define SGFIM_KERNEL_STREAM 3  /* one warp per candidate, rows streamed from L2/HBM */
+int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves);
+
 /* Allocation-free form of sgfim_support_batch_device.  It has no counterpart
  * in the reference; it exists for callers that must not allocate device
  * memory: applications whose own memory pool owns the GPU and forbids other
  * code to call cudaMalloc/cudaFree (for example a serving process that plans
  * all of its HBM at start-up), or hot loops that cannot afford cudaMalloc's
  * implicit synchronisation.  It needs no handle and allocates nothing; its
- * scratch is a fixed array in the library's device memory (about 21 MB, kept
+ * scratch is a fixed array in the library's device memory (about 25 MB, kept
  * by every GPU that loads the library until the process exits).
  *   - Arguments and results are those of sgfim_support_batch_device
  *     (device pointers, asynchronous on `stream`, the current CUDA device).
@@ -196,16 +208,28 @@ typedef struct {
     uint64_t waves;          /* device waves */
     uint64_t kernel_launches;
     uint64_t candidates;     /* candidate MFIs emitted before the final maximality filter */
+    /* search trace (sgfim_mine_params.record_trace): one row per created child
+     * node -- trace_dim features (SGFIM_TRACE_DIM, see sgfim/mlp.py FEATURES) and
+     * label 1 when a final MFI was emitted inside that child's subtree */
+    uint64_t trace_n;
+    uint32_t trace_dim;
+    float *trace_features;   /* trace_n * trace_dim */
+    uint8_t *trace_labels;   /* trace_n */
 } sgfim_result;
+
+#define SGFIM_TRACE_DIM 8
 
 /* Root rules: which items may be the highest-id item of a reported MFI. */
 #define SGFIM_ROOTS_ALL 0     /* every frequent item: the complete MFI set (mine_mfi, skab_spike.py:84-135) */
 #define SGFIM_ROOTS_LIST 1    /* the ids in `roots` (AnyFIM stage k: the top-k ids, AnytimeMining/kernel.cu:850-859) */
 #define SGFIM_ROOTS_MINCOUNT 2 /* ids with count >= root_min_count (TensorFIM: count/n > thr, kernel_bmma.cu:1199,1224-1233) */
 
-/* Frontier orders (change the order of emission, never the result). */
-#define SGFIM_ORDER_SUPPORT 0 /* canonical: tail items by ascending support */
-#define SGFIM_ORDER_LEARNED 1 /* priority from the loaded scoring MLP */
+/* Frontier orders: the order in which sibling subtrees are searched.  The
+ * tree itself (every node's tail: the frequent extensions of higher support)
+ * and the final result never change; only the emission order does. */
+#define SGFIM_ORDER_SUPPORT 0      /* canonical: lowest-support sibling first */
+#define SGFIM_ORDER_LEARNED 1      /* highest score of the loaded scoring MLP first */
+#define SGFIM_ORDER_SUPPORT_DESC 2 /* highest-support sibling first (the reference's frequency order) */
 
 typedef struct {
     uint32_t min_count;       /* absolute support threshold (>= 1) */
@@ -216,6 +240,7 @@ typedef struct {
     uint32_t order;           /* SGFIM_ORDER_* */
     double time_limit_s;      /* 0 = none; expiry returns SGFIM_ETIMEDOUT */
     uint64_t node_limit;      /* 0 = none; exceeding it returns SGFIM_ENOMEM */
+    uint32_t record_trace;    /* non-zero: fill the result's trace arrays */
 } sgfim_mine_params;
 
 /* Exact MFI set {M in MFI(min_count) : max(M) in roots}.  With
@@ -270,6 +295,28 @@ typedef struct {
 } sgfim_af_meta;
 int sgfim_write_anyfim(sgfim_handle *h, sgfim_result *const *stages, const sgfim_af_meta *meta,
                        const char *path);
+
+/* ---------------------------------------------------------------- windows */
+
+/* Device-resident transaction ring for sliding-window mining (no reference
+ * counterpart; the reference transactionises windows on the host,
+ * code/pipeline/skab_spike.py:61-80, and runs one engine process per file).
+ * Items are ids 0..n_items-1; the ring keeps the newest `capacity` (rounded up
+ * to a power of two of 64) transactions as vertical bitmap rows on the GPU.
+ * Appending a batch evicts the oldest transactions it overwrites.  Thread
+ * safe: appends and window loads may come from different host threads. */
+typedef struct sgfim_ring sgfim_ring;
+int sgfim_ring_open(int device, uint32_t n_items, uint64_t capacity_txn, sgfim_ring **out);
+void sgfim_ring_close(sgfim_ring *r);
+/* Stream position of the next transaction (= transactions appended so far). */
+uint64_t sgfim_ring_head(sgfim_ring *r);
+uint64_t sgfim_ring_capacity(const sgfim_ring *r);
+/* Append n_txn transactions (CSR over item ids; ids >= n_items are ignored). */
+int sgfim_ring_append(sgfim_ring *r, const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn);
+/* Make the window [start, start+len) of the stream the handle's dataset
+ * (bitmaps copied on the device; rows = item ids).  The window must still be
+ * in the ring: head - start <= capacity and start + len <= head. */
+int sgfim_ring_window_load(sgfim_ring *r, sgfim_handle *h, uint64_t start, uint64_t len);
 
 /* ---------------------------------------------------------------- scoring */
 

@@ -28,6 +28,28 @@ def test_support_batch_matches_oracle(engine, n_txn, d, n_cand, kmin, kmax):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("kernel", ["sorted", "staged", "stream"])
+@pytest.mark.parametrize("d", [1024, 300])
+def test_support_kernels_agree(engine, kernel, d):
+    """Every kernel plan gives the oracle's supports (k = 0..12, unknown ids included)."""
+    n_txn = 32 * 1024 + 64
+    bm = _bitmaps(n_txn, d, seed=d + 5)
+    engine.load_bitmaps(bm, n_txn)
+    cp, ci = datagen.walk_candidates(12000, d, 1, 12, seed=11)
+    # prepend an empty candidate and one with an unknown id
+    cp = np.concatenate([[0, 0, 2], cp + 2]).astype(np.uint64)
+    ci = np.concatenate([[3, d + 7], ci]).astype(np.uint32)
+    try:
+        for cpc, waves in [(0, 0), (777, 0), (0, 5)]:
+            engine.set_support_plan(kernel, cpc, waves)
+            got = engine.support_batch(cp, ci)
+            want = oracle.support_batch(bm, cp[2:] - 2, ci[2:])
+            assert got[0] == n_txn and got[1] == 0
+            assert np.array_equal(got[2:], want), (kernel, cpc, waves)
+    finally:
+        engine.set_support_plan("auto")
+
+
 def test_support_batch_edge_candidates(engine):
     n_txn, d = 8192, 50
     bm = _bitmaps(n_txn, d, seed=1)
@@ -92,8 +114,8 @@ def test_support_full_size_sample(engine):
     assert (parent >= got).all()
 
 
-@pytest.mark.parametrize("kind", [1, 2])
-@pytest.mark.parametrize("n_txn,d", [(4096, 24), (65536 + 64, 300), (1 << 16, 256)])
+@pytest.mark.parametrize("kind", [1, 2, 3])
+@pytest.mark.parametrize("n_txn,d", [(4096, 24), (65536 + 64, 300), (1 << 16, 256), (100_032, 130)])
 def test_cooccurrence_matches_oracle(engine, kind, n_txn, d):
     torch = pytest.importorskip("torch")
     bm = _bitmaps(n_txn, d, seed=d + kind)

@@ -128,6 +128,25 @@ def test_anytime_checkpoints(engine):
     assert final == {frozenset(s): c for s, c in ref}
 
 
+def test_orders_give_identical_sets_and_traces(engine):
+    """Frontier orders change only the emission order; traces label the nodes on
+    the path to every final MFI."""
+    rows = datagen.regime_txns(40_000, 30, 8, 32, 0.2, seed=13)
+    engine.load_rows(rows)
+    thr = int(0.03 * 40_000)
+    base = engine.mine(thr, record_trace=True)
+    assert base.trace_features.shape[1] == 8 and len(base.trace_labels) == len(base.trace_features)
+    assert 0 < base.trace_labels.mean() < 1
+    desc = engine.mine(thr, order="support_desc")
+    assert desc.as_dict() == base.as_dict()
+    # a scorer with random weights still gives the exact set
+    rng = np.random.default_rng(0)
+    engine.load_scorer(rng.normal(0, .3, (128, 8)), np.zeros(128), rng.normal(0, .1, (128, 128)), np.zeros(128),
+                       rng.normal(0, .1, 128), np.zeros(1))
+    learned = engine.mine(thr, order="learned")
+    assert learned.as_dict() == base.as_dict()
+
+
 def test_cancel_from_checkpoint(engine):
     from sgfim.engine import SgfimError
     rows = datagen.regime_txns(30_000, 30, 8, 32, 0.2, seed=9)

@@ -80,11 +80,11 @@ struct Staged {
 struct MinerWorkspace {
     DevBuf arena, pool, q_out, score, cooc;
     HostBuf hq_out, hscore;
-    Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat;
+    Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat, w0;
     void release() {
         arena.release(); pool.release(); q_out.release(); score.release(); cooc.release();
         hq_out.release(); hscore.release();
-        for (Staged *s : {&q_ptr, &q_items, &q_slot, &c_ptr, &c_items, &c_ps, &c_cs, &p_ptr, &p_items, &feat})
+        for (Staged *s : {&q_ptr, &q_items, &q_slot, &c_ptr, &c_items, &c_ps, &c_cs, &p_ptr, &p_items, &feat, &w0})
             s->release();
     }
 };

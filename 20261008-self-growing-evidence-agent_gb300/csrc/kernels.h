@@ -9,8 +9,10 @@ namespace sg {
 
 constexpr uint32_t kNoSlot = 0xffffffffu;
 
-// Counting modes of the streaming query kernel.
-enum QueryMode : int { QUERY_COUNT = 0, QUERY_ANY = 1 };
+// Counting modes of the streaming query kernel.  QUERY_ANY stops at the first
+// set bit (result 0 / non-zero); QUERY_ANY2 stops once two bits are counted
+// (result 0, 1 or >= 2).
+enum QueryMode : int { QUERY_COUNT = 0, QUERY_ANY = 1, QUERY_ANY2 = 2 };
 
 // A batch of AND-popcount queries over row-major uint64 bitmaps.
 // Query q: popc(mask_q & AND_{i in items[ptr[q]..ptr[q+1])} rows[i]) over
@@ -30,6 +32,7 @@ struct QueryBatch {
     uint64_t n_q = 0;
     const uint64_t *n_q_device = nullptr;  // when set, the query count is read on the device
     const uint32_t *q_index = nullptr;     // optional indirection: query j is q_index[j]
+    const uint64_t *q_w0 = nullptr;        // optional first word of each query (words before it are skipped)
     uint32_t *out = nullptr;
     uint64_t empty_value = 0;       // result of an empty query without mask
     int mode = QUERY_COUNT;

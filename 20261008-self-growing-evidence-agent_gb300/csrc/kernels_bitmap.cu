@@ -161,7 +161,8 @@ __global__ void __launch_bounds__(256) query_kernel(QueryBatch qb) {
             continue;
         }
         uint32_t acc = 0;
-        for (uint64_t base = 0; base < qb.n_words; base += 64) {
+        const uint64_t w_first = qb.q_w0 ? (qb.q_w0[q] & ~1ull) : 0;
+        for (uint64_t base = w_first; base < qb.n_words; base += 64) {
             const uint64_t w = base + 2 * lane;
             if (w < qb.n_words) {
                 uint4 v = mask ? ld_nc_v4(mask + w) : make_uint4(~0u, ~0u, ~0u, ~0u);
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(256) query_kernel(QueryBatch qb) {
                 acc += popc4(v);
             }
             if (qb.mode == QUERY_ANY && __any_sync(0xffffffffu, acc != 0)) break;
+            if (qb.mode == QUERY_ANY2 && __reduce_add_sync(0xffffffffu, acc) >= 2) break;
         }
         acc = warp_sum(acc);
         if (lane == 0) qb.out[q] = acc;

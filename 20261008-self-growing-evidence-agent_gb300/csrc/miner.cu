@@ -73,7 +73,7 @@ class Miner {
     Miner(sgfim_handle *h, const sgfim_mine_params &p)
         : h_(h), ds_(h->ds), p_(p), w_(h->mws), arena_(w_.arena), pool_(w_.pool), q_ptr_(w_.q_ptr),
           q_items_(w_.q_items), q_slot_(w_.q_slot), c_ptr_(w_.c_ptr), c_items_(w_.c_items), c_ps_(w_.c_ps),
-          c_cs_(w_.c_cs), p_ptr_(w_.p_ptr), p_items_(w_.p_items), feat_(w_.feat), q_out_(w_.q_out),
+          c_cs_(w_.c_cs), p_ptr_(w_.p_ptr), p_items_(w_.p_items), feat_(w_.feat), w0_(w_.w0), q_out_(w_.q_out),
           score_(w_.score), hq_out_(w_.hq_out), hscore_(w_.hscore) {}
 
     int run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out);
@@ -99,6 +99,7 @@ class Miner {
     std::vector<uint32_t> csup_;
     std::vector<double> ctime_;
     std::vector<uint32_t> cnode_;
+    std::vector<uint64_t> ccheck_;   // pool size when the candidate was tested against the pool
     // search tree and trace
     std::vector<uint32_t> parent_;
     std::vector<float> tfeat_;
@@ -106,7 +107,7 @@ class Miner {
     bool need_feat_ = false;
     std::vector<uint32_t> cooc_;
     // staging (workspace)
-    Staged &q_ptr_, &q_items_, &q_slot_, &c_ptr_, &c_items_, &c_ps_, &c_cs_, &p_ptr_, &p_items_, &feat_;
+    Staged &q_ptr_, &q_items_, &q_slot_, &c_ptr_, &c_items_, &c_ps_, &c_cs_, &p_ptr_, &p_items_, &feat_, &w0_;
     DevBuf &q_out_, &score_;
     HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
@@ -119,7 +120,7 @@ class Miner {
         return s;
     }
     void run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
-                     int mode, std::vector<uint32_t> &out);
+                     int mode, std::vector<uint32_t> &out, const uint64_t *w0 = nullptr);
     void pool_reserve(uint64_t members);
     void emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node);
     void flush_pool(uint64_t from);
@@ -131,7 +132,7 @@ class Miner {
 };
 
 void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
-                        int mode, std::vector<uint32_t> &out) {
+                        int mode, std::vector<uint32_t> &out, const uint64_t *w0) {
     const size_t n = qs.size();
     out.assign(n, 0);
     if (n == 0) return;
@@ -140,6 +141,7 @@ void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t strid
     qb.q_ptr = q_ptr_.put(qs.ptr.data(), n + 1, st);
     qb.q_items = q_items_.put(qs.items.data(), qs.items.size(), st);
     qb.mask_slot = q_slot_.put(qs.slot.data(), n, st);
+    if (w0) qb.q_w0 = w0_.put(w0, n, st);
     q_out_.reserve(n * 4, st);
     hq_out_.reserve(n * 4);
     qb.rows = rows; qb.row_stride = stride; qb.n_words = n_words; qb.d = d;
@@ -188,6 +190,7 @@ void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node) 
     csup_.push_back(sup);
     ctime_.push_back(elapsed());
     cnode_.push_back(node);
+    ccheck_.push_back(pool_n_);
 }
 
 // Append candidates [from, n) to the device pool (asynchronous; the next
@@ -325,9 +328,18 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     };
     std::vector<Work> work;
     std::vector<MNode> kids;
-    std::vector<uint32_t> child_parent, child_slot;
+    std::vector<std::pair<uint32_t, uint32_t>> kid_src;  // (parent slot, added item)
+    std::vector<uint32_t> child_slot;
 
-    while (!stack.empty()) {
+    // Learned order: children scored below kDeferBelow wait on a deferred stack,
+    // searched once the main stack is empty (they keep no tidset mask meanwhile).
+    std::vector<MNode> deferred;
+    constexpr float kDeferBelow = 0.5f;
+    while (!stack.empty() || !deferred.empty()) {
+        if (stack.empty()) {
+            // hand the deferred subtrees back, highest score first on top
+            std::swap(stack, deferred);
+        }
         // ---- pop a wave
         wave.clear();
         uint64_t nq = 0;
@@ -340,6 +352,27 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         ++waves_;
         nodes_ += wave.size();
+        // nodes without a mask (deferred, or created when the arena was full) get
+        // one rebuilt from their head rows when a slot is free
+        qchild.clear();
+        child_slot.clear();
+        for (MNode &nd : wave) {
+            if (nd.slot != kNoSlot || nd.head.empty() || nd.tail.size() < 2) continue;
+            const uint32_t s = alloc_slot();
+            if (s == kNoSlot) break;
+            qchild.add(nd.head.data(), nd.head.size(), kNoSlot);
+            child_slot.push_back(s);
+            nd.slot = s;
+        }
+        if (qchild.size()) {
+            const size_t n = qchild.size();
+            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(),
+                               ds_.stride, c_ptr_.put(qchild.ptr.data(), n + 1, st),
+                               c_items_.put(qchild.items.data(), qchild.items.size(), st),
+                               c_ps_.put(qchild.slot.data(), n, st), c_cs_.put(child_slot.data(), n, st), (uint32_t)n,
+                               st, h_->n_sm);
+            ++launches_;
+        }
         // ---- phase A: s_e for every tail item
         qs.clear();
         for (const MNode &nd : wave) {
@@ -393,9 +426,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt);
         // ---- phase C: emit candidates, create children
         const uint64_t pool_before = csup_.size();
-        qchild.clear();
-        child_slot.clear();
         kids.clear();
+        kid_src.clear();
         wfeat.clear();
         for (size_t i = 0; i < wave.size(); ++i) {
             MNode &nd = wave[i];
@@ -432,23 +464,28 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                         tnode_.push_back(c.id);
                     }
                 }
-                if (!c.tail.empty()) {
-                    // a child without tail is a leaf: its own wave tests it against the pool
-                    c.slot = alloc_slot();
-                    if (c.slot != kNoSlot) {
-                        if (nd.slot != kNoSlot) {
-                            const uint32_t e = wk.f[j].second;
-                            qchild.add(&e, 1, nd.slot);
-                        } else {
-                            qchild.add(c.head.data(), c.head.size(), kNoSlot);
-                        }
-                        child_slot.push_back(c.slot);
-                    }
-                }
+                kid_src.emplace_back(nd.slot, wk.f[j].second);
                 kids.push_back(std::move(c));
             }
         }
-        // child masks: mask(child) = mask(parent) & AND rows(list)
+        // learned order: score every child of the wave in one launch
+        std::vector<uint8_t> defer(kids.size(), 0);
+        if (p_.order == SGFIM_ORDER_LEARNED) {
+            score(wfeat, kids.size(), wscore);
+            for (size_t k = 0; k < kids.size(); ++k) defer[k] = wscore[k] < kDeferBelow;
+        }
+        // child masks for the children searched next: mask(child) = mask(parent) & row(e)
+        qchild.clear();
+        child_slot.clear();
+        for (size_t k = 0; k < kids.size(); ++k) {
+            MNode &c = kids[k];
+            if (c.tail.empty() || defer[k]) continue;  // leaves need no mask; deferred ones rebuild theirs
+            c.slot = alloc_slot();
+            if (c.slot == kNoSlot) continue;
+            if (kid_src[k].first != kNoSlot) qchild.add(&kid_src[k].second, 1, kid_src[k].first);
+            else qchild.add(c.head.data(), c.head.size(), kNoSlot);
+            child_slot.push_back(c.slot);
+        }
         if (qchild.size()) {
             const size_t n = qchild.size();
             const uint64_t *dptr = c_ptr_.put(qchild.ptr.data(), n + 1, st);
@@ -459,8 +496,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                                ds_.stride, dptr, ditems, dps, dcs, (uint32_t)n, st, h_->n_sm);
             ++launches_;
         }
-        // sibling visiting order
-        if (p_.order == SGFIM_ORDER_LEARNED) score(wfeat, kids.size(), wscore);
+        // sibling visiting order; deferred children go to the deferred stack
         for (size_t i = wave.size(); i-- > 0;) {
             // stack is LIFO: nodes pushed later are popped first; keep wave order
             Work &wk = work[i];
@@ -472,7 +508,10 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             } else if (p_.order == SGFIM_ORDER_LEARNED) {
                 std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return wscore[a] > wscore[b]; });
             }
-            for (size_t j = ord.size(); j-- > 0;) stack.push_back(std::move(kids[ord[j]]));
+            for (size_t j = ord.size(); j-- > 0;) {
+                if (defer[ord[j]]) deferred.push_back(std::move(kids[ord[j]]));
+                else stack.push_back(std::move(kids[ord[j]]));
+            }
         }
         // parents' masks are no longer needed once the child-mask kernel ran (stream order)
         for (MNode &nd : wave)
@@ -540,18 +579,25 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
 
 int Miner::finish(sgfim_result **out) {
     const uint64_t n = csup_.size();
-    // maximality filter: members of the pool containing each candidate
+    // maximality filter: a candidate was already tested against every member
+    // that existed when it was found, so only later members (its own bit
+    // included) can contain it; two hits mean a proper superset exists
     std::vector<uint8_t> keep(n, 1);
     if (n > 1) {
         const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
         const uint64_t chunk = 1u << 20;
         QuerySet qs;
         std::vector<uint32_t> cnt;
+        std::vector<uint64_t> w0;
         for (uint64_t a = 0; a < n; a += chunk) {
             const uint64_t b = std::min(n, a + chunk);
             qs.clear();
-            for (uint64_t c = a; c < b; ++c) qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
-            run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_COUNT, cnt);
+            w0.clear();
+            for (uint64_t c = a; c < b; ++c) {
+                qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
+                w0.push_back(ccheck_[c] / 64);
+            }
+            run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_ANY2, cnt, w0.data());
             for (uint64_t c = a; c < b; ++c) keep[c] = cnt[c - a] <= 1;
         }
     }

@@ -1,0 +1,117 @@
+"""Autotuner for the batched support kernels and the co-occurrence kernels.
+
+The reference tunes its wave engine by hand: run_ablation.py sweeps the
+BMMA_WAVE_CAP / BMMA_SPLITK_OFF / BMMA_MASK_WPB environment variables
+(code/engine_tensorfim/scripts/run_ablation.py:15-22, kernel_bmma.cu:351-368)
+and checks that every setting still gives the gold MFI set.  Here the sweep is
+part of the library's Python layer: each candidate plan (kernel kind x CTA
+sizing) is timed with CUDA events on the caller's device buffers, results are
+required to be identical across plans, and the winner is cached in a JSON
+file keyed by device, item count and size buckets.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+SUPPORT_PLANS = [("staged", 0, 0), ("staged", 0, 1), ("staged", 0, 3), ("sorted", 0, 0), ("sorted", 0, 2),
+                 ("stream", 0, 0)]
+COOC_KINDS = [(1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3")]
+
+
+def _bucket(x):
+    return 1 << max(0, int(math.ceil(math.log2(max(int(x), 1)))))
+
+
+def cache_key(device_name, kind, d, n_words, n_cand=0):
+    return f"{device_name}|{kind}|d={d}|w={_bucket(n_words)}|n={_bucket(n_cand)}"
+
+
+class Autotuner:
+    def __init__(self, engine, cache_path=None):
+        import torch
+        self.torch = torch
+        self.eng = engine
+        self.path = cache_path
+        self.cache = {}
+        if cache_path and os.path.exists(cache_path):
+            with open(cache_path) as f:
+                self.cache = json.load(f)
+
+    def _save(self):
+        if self.path:
+            with open(self.path, "w") as f:
+                json.dump(self.cache, f, indent=1)
+
+    def _time(self, fn, reps=3):
+        torch = self.torch
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        return best
+
+    def tune_support(self, bm, d, n_words, row_stride, cand_ptr, cand_items, n_cand, out, plans=SUPPORT_PLANS):
+        """bm/cand_ptr/cand_items/out: torch CUDA tensors.  Returns (best plan, timings);
+        the best plan is left active on the engine."""
+        torch = self.torch
+        key = cache_key(torch.cuda.get_device_name(), "support", d, n_words, n_cand)
+        if key in self.cache:
+            p = self.cache[key]["best"]
+            self.eng.set_support_plan(*p)
+            return tuple(p), self.cache[key]["ms"]
+        stream = torch.cuda.current_stream().cuda_stream
+        ref = None
+        timings = {}
+        for kernel, cpc, waves in plans:
+            if kernel == "sorted" and d > 1024:
+                continue
+            self.eng.set_support_plan(kernel, cpc, waves)
+
+            def run():
+                self.eng.support_batch_device(bm.data_ptr(), d, n_words, row_stride, cand_ptr.data_ptr(),
+                                              cand_items.data_ptr(), n_cand, out.data_ptr(), stream)
+            ms = self._time(run)
+            res = out.clone()
+            if ref is None:
+                ref = res
+            elif not torch.equal(ref, res):
+                raise RuntimeError(f"plan {(kernel, cpc, waves)} changed the supports")
+            timings[f"{kernel}/cpc={cpc}/waves={waves}"] = ms
+        best_name = min(timings, key=timings.get)
+        kernel, cpc_s, waves_s = best_name.split("/")
+        best = (kernel, int(cpc_s.split("=")[1]), int(waves_s.split("=")[1]))
+        self.eng.set_support_plan(*best)
+        self.cache[key] = {"best": list(best), "ms": timings}
+        self._save()
+        return best, timings
+
+    def tune_cooc(self, bm, d, n_words, row_stride, out, kinds=COOC_KINDS):
+        torch = self.torch
+        key = cache_key(torch.cuda.get_device_name(), "cooc", d, n_words)
+        if key in self.cache:
+            return self.cache[key]["best"], self.cache[key]["ms"]
+        stream = torch.cuda.current_stream().cuda_stream
+        ref = None
+        timings = {}
+        for kind, name in kinds:
+            def run():
+                self.eng.cooccurrence_device(bm.data_ptr(), d, n_words, row_stride, out.data_ptr(), kind, stream)
+            timings[name] = self._time(run)
+            res = out.clone()
+            if ref is None:
+                ref = res
+            elif not torch.equal(ref, res):
+                raise RuntimeError(f"co-occurrence kernel {name} disagrees")
+        best = min(timings, key=timings.get)
+        self.cache[key] = {"best": best, "ms": timings}
+        self._save()
+        return best, timings

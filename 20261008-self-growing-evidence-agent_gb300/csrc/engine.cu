@@ -120,6 +120,8 @@ int sgfim_open(const sgfim_config *cfg, sgfim_handle **out) {
     SG_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     SG_CUDA_TRY(cudaEventCreate(&h->ev_a));
     SG_CUDA_TRY(cudaEventCreate(&h->ev_b));
+    if (cfg && (cfg->flags & SGFIM_F_BLOCKING_SYNC))
+        SG_CUDA_TRY(cudaEventCreateWithFlags(&h->ev_sync, cudaEventBlockingSync | cudaEventDisableTiming));
     size_t free_b = 0, total_b = 0;
     SG_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     h->hbm_budget = (cfg && cfg->hbm_budget) ? cfg->hbm_budget : (uint64_t)(free_b * 0.9);
@@ -157,6 +159,7 @@ void sgfim_close(sgfim_handle *h) {
         for (auto &e : q.e) cudaEventDestroy(e);
     for (auto &q : h->timer_free)
         for (auto &e : q.e) cudaEventDestroy(e);
+    if (h->ev_sync) cudaEventDestroy(h->ev_sync);
     if (h->ev_a) cudaEventDestroy(h->ev_a);
     if (h->ev_b) cudaEventDestroy(h->ev_b);
     if (h->stream) cudaStreamDestroy(h->stream);

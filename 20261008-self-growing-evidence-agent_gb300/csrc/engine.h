@@ -115,6 +115,16 @@ struct sgfim_handle {
     sg::SupportPlan plan;
     uint64_t launches = 0;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev_sync = nullptr;   // blocking-sync event (SGFIM_F_BLOCKING_SYNC)
+    // wait for all work queued on the handle's stream
+    void sync() {
+        if (ev_sync) {
+            SG_CUDA_TRY(cudaEventRecord(ev_sync, stream));
+            SG_CUDA_TRY(cudaEventSynchronize(ev_sync));
+        } else {
+            SG_CUDA_TRY(cudaStreamSynchronize(stream));
+        }
+    }
     // phase timers: event quads recorded by timed calls, resolved by sgfim_phase_stats_get
     struct Quad { cudaEvent_t e[4]; };
     std::vector<Quad> timer_busy, timer_free;

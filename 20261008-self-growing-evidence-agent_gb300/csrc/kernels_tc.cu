@@ -27,7 +27,7 @@ namespace sg {
 namespace {
 
 constexpr int kTcThreads = 256;
-constexpr int kTcStages = 3;
+constexpr int kTcStages = 2;
 constexpr int kTcAtom = 128 * 128;             // one 128-row x 128-byte swizzle atom
 constexpr int kTcOperand = 2 * kTcAtom;        // two atoms along K per operand
 constexpr int kTcStageBytes = 2 * kTcOperand;  // A and B
@@ -86,11 +86,21 @@ __device__ __forceinline__ void expand_row(uint8_t *atom, uint32_t r, uint64_t l
     }
 }
 
+// Bit slices arrive by TMA (box 4 words x 128 rows per operand) into a ring of
+// kTcRing slots issued kTcRing steps ahead; expansion reads them from shared
+// memory, and the two fp8 stages alternate so that expanding step i+1
+// overlaps the tensor core's MMAs on step i.
+constexpr int kTcRing = 6;
+constexpr int kTcBitTile = 128 * 32;       // one operand's bit slice: 128 rows x 4 words
+constexpr int kTcBitSlot = 2 * kTcBitTile;
+
 __global__ void __launch_bounds__(kTcThreads, 1)
-    cooc_tc_kernel(const uint64_t *__restrict__ bm, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t n_tiles,
+    cooc_tc_kernel(const __grid_constant__ CUtensorMap bm_map, uint64_t n_words, uint32_t d, uint32_t n_tiles,
                    uint64_t words_per_split, uint32_t *__restrict__ out, uint32_t *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t bars[kTcStages + 1];
+    __shared__ uint64_t mma_bar[kTcStages];
+    __shared__ uint64_t bit_bar[kTcRing];
+    __shared__ uint64_t done_bar;
     __shared__ uint32_t tmem_slot;
     uint32_t t = blockIdx.x, bi = 0;
     while (t >= n_tiles - bi) { t -= n_tiles - bi; ++bi; }
@@ -98,8 +108,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint64_t w_begin = (uint64_t)blockIdx.y * words_per_split;
     const uint64_t w_end = min(n_words, w_begin + words_per_split);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    // 1024-byte aligned stage base (SWIZZLE_128B atoms)
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem) + 1023) & ~uintptr_t(1023));
+    uint8_t *ring = base + (size_t)kTcStages * kTcStageBytes;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
@@ -108,7 +118,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s <= kTcStages; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < kTcStages; ++s) mbar_init(&mma_bar[s], 1);
+        for (int s = 0; s < kTcRing; ++s) mbar_init(&bit_bar[s], 1);
+        mbar_init(&done_bar, 1);
         fence_mbar_init();
     }
     tc_fence_before();
@@ -117,37 +129,35 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t tmem = tmem_slot;
 
     const uint64_t n_steps = w_begin < w_end ? (w_end - w_begin + 3) / 4 : 0;  // 4 words = 256 bits per step
+    auto issue = [&](uint64_t step) {
+        const uint32_t slot = (uint32_t)(step % kTcRing);
+        uint8_t *dst = ring + (size_t)slot * kTcBitSlot;
+        mbar_arrive_expect_tx(&bit_bar[slot], kTcBitSlot);
+        const int32_t x = (int32_t)(w_begin + step * 4);
+        tma_load_2d(dst, &bm_map, x, (int32_t)(bi * 128), &bit_bar[slot]);
+        tma_load_2d(dst + kTcBitTile, &bm_map, x, (int32_t)(bj * 128), &bit_bar[slot]);
+    };
+    if (tid == 0)
+        for (uint64_t sidx = 0; sidx < n_steps && sidx < (uint64_t)kTcRing; ++sidx) issue(sidx);
     bool ok = true;
     for (uint64_t it = 0; it < n_steps; ++it) {
+        const uint32_t slot = (uint32_t)(it % kTcRing);
         const uint32_t s = (uint32_t)(it % kTcStages);
         uint8_t *stage = base + (size_t)s * kTcStageBytes;
-        if (it >= kTcStages) {
-            // the MMAs that read this stage kStages steps ago must be done
-            ok = mbar_wait_bounded(&bars[s], (uint32_t)((it / kTcStages - 1) & 1), err);
-        }
+        ok = mbar_wait_bounded(&bit_bar[slot], (uint32_t)((it / kTcRing) & 1), err);
+        if (ok && it >= kTcStages)
+            ok = mbar_wait_bounded(&mma_bar[s], (uint32_t)((it / kTcStages - 1) & 1), err);
         if (__syncthreads_or(!ok)) break;
-        // expand: thread -> one row of A (tid < 128) or B (tid >= 128), 256 bits
         {
+            // thread -> one row of A (tid < 128) or B (tid >= 128): 4 words from the ring
             const uint32_t r = tid & 127;
-            const uint32_t row = (tid < 128 ? bi : bj) * 128 + r;
+            const uint8_t *src = ring + (size_t)slot * kTcBitSlot + (tid < 128 ? 0 : kTcBitTile) + r * 32;
+            const uint4 x0 = *reinterpret_cast<const uint4 *>(src);
+            const uint4 x1 = *reinterpret_cast<const uint4 *>(src + 16);
             uint8_t *op = stage + (tid < 128 ? 0 : kTcOperand);
-            const uint64_t w0 = w_begin + it * 4;
-            uint64_t v[4] = {0, 0, 0, 0};
-            if (row < d) {
-                const uint64_t *src = bm + (uint64_t)row * stride + w0;
-                if (w0 + 3 < w_end) {
-                    const uint4 a = ld_nc_v4(src), b = ld_nc_v4(src + 2);
-                    v[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
-                    v[1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
-                    v[2] = (uint64_t)b.x | ((uint64_t)b.y << 32);
-                    v[3] = (uint64_t)b.z | ((uint64_t)b.w << 32);
-                } else {
-                    for (int q = 0; q < 4; ++q)
-                        if (w0 + q < w_end) v[q] = src[q];
-                }
-            }
-            expand_row(op, r, v[0], v[1]);
-            expand_row(op + kTcAtom, r, v[2], v[3]);
+            expand_row(op, r, (uint64_t)x0.x | ((uint64_t)x0.y << 32), (uint64_t)x0.z | ((uint64_t)x0.w << 32));
+            expand_row(op + kTcAtom, r, (uint64_t)x1.x | ((uint64_t)x1.y << 32),
+                       (uint64_t)x1.z | ((uint64_t)x1.w << 32));
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -159,15 +169,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const uint32_t off = (uint32_t)(k >> 2) * kTcAtom + (uint32_t)(k & 3) * 32;
                 tc_mma(tmem, smem_desc_sw128(a0 + off), smem_desc_sw128(b0 + off), (it > 0 || k > 0) ? 1u : 0u);
             }
-            tc_commit(&bars[s]);
+            tc_commit(&mma_bar[s]);
+            // every thread has read this ring slot: refill it kTcRing steps ahead
+            if (it + kTcRing < n_steps) issue(it + kTcRing);
         }
     }
     // wait for every MMA before reading the accumulator
-    if (tid == 0) {
-        if (n_steps > 0) tc_commit(&bars[kTcStages]);
-    }
+    if (tid == 0 && n_steps > 0) tc_commit(&done_bar);
     __syncthreads();
-    if (ok && n_steps > 0) ok = mbar_wait_bounded(&bars[kTcStages], 0, err);
+    if (ok && n_steps > 0) ok = mbar_wait_bounded(&done_bar, 0, err);
     tc_fence_after();
     if (__syncthreads_or(!ok) == 0 && n_steps > 0 && warp < 4) {
         const uint32_t lane_base = warp * 32;
@@ -200,6 +210,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         }
     }
+    if (!ok) {
+        // let copies still in flight land before the CTA's shared memory goes away
+        for (int sidx = 0; sidx < kTcRing; ++sidx) mbar_wait_bounded(&bit_bar[sidx], 0, err);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -208,9 +222,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
+bool encode_bits_map(CUtensorMap *map, const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride) {
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return false;
+        fn = reinterpret_cast<EncodeFn>(p);
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)n_words, (cuuint64_t)d};
+    cuuint64_t strides[1] = {(cuuint64_t)row_stride * 8};
+    cuuint32_t box[2] = {4, 128};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<uint64_t *>(bitmaps), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
-size_t tc_smem_bytes() { return (size_t)kTcStages * kTcStageBytes + 1024; }
+size_t tc_smem_bytes() { return (size_t)kTcStages * kTcStageBytes + (size_t)kTcRing * kTcBitSlot + 1024; }
 
 int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
                    cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches) {
@@ -226,10 +263,12 @@ int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64
     wps = std::min<uint64_t>(wps, (1ull << 20) / 64);
     wps = (wps + 3) / 4 * 4;
     splits = (n_words + wps - 1) / wps;
+    CUtensorMap map;
+    if (!encode_bits_map(&map, bitmaps, d, n_words, row_stride)) return -1;
     const size_t smem = tc_smem_bytes();
     SG_CUDA_TRY(cudaFuncSetAttribute(cooc_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(pairs, (unsigned)splits);
-    cooc_tc_kernel<<<grid, kTcThreads, smem, st>>>(bitmaps, row_stride, n_words, d, n_tiles, wps, out, dev_err);
+    cooc_tc_kernel<<<grid, kTcThreads, smem, st>>>(map, n_words, d, n_tiles, wps, out, dev_err);
     SG_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 1;
     return 0;

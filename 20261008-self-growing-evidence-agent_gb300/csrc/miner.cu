@@ -111,6 +111,13 @@ class Miner {
     DevBuf &q_out_, &score_;
     HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
+    double phase_[6] = {0, 0, 0, 0, 0, 0};   // see sgfim_result.phase_s
+    // adds the wall time of f() to phase_[i]
+    template <class F> void timed(int i, F &&f) {
+        const auto a = Clock::now();
+        f();
+        phase_[i] += std::chrono::duration<double>(Clock::now() - a).count();
+    }
 
     double elapsed() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
     uint32_t alloc_slot() {
@@ -150,7 +157,7 @@ void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t strid
     launch_queries(qb, st, h_->n_sm);
     ++launches_;
     SG_CUDA_TRY(cudaMemcpyAsync(hq_out_.ptr, q_out_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
-    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    h_->sync();
     memcpy(out.data(), hq_out_.ptr, n * 4);
 }
 
@@ -263,7 +270,7 @@ void Miner::score(const std::vector<float> &feat, size_t n, std::vector<float> &
                        score_.as<float>(), st);
     ++launches_;
     SG_CUDA_TRY(cudaMemcpyAsync(hscore_.ptr, score_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
-    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    h_->sync();
     memcpy(out.data(), hscore_.ptr, n * 4);
 }
 
@@ -386,7 +393,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 }
             }
         }
-        run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts);
+        timed(0, [&] { run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts); });
         // ---- phase B: PEP, ordering, pool and FHUT queries
         work.assign(wave.size(), Work{});
         qpool.clear();
@@ -419,11 +426,11 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         if (pool_n_ > 0) {
             const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
-            run_queries(qpool, pool_.as<uint64_t>(), pool_words_, pw, d, QUERY_ANY, pool_hit);
+            timed(1, [&] { run_queries(qpool, pool_.as<uint64_t>(), pool_words_, pw, d, QUERY_ANY, pool_hit); });
         } else {
             pool_hit.assign(qpool.size(), 0);
         }
-        run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt);
+        timed(2, [&] { run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt); });
         // ---- phase C: emit candidates, create children
         const uint64_t pool_before = csup_.size();
         kids.clear();
@@ -471,7 +478,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         // learned order: score every child of the wave in one launch
         std::vector<uint8_t> defer(kids.size(), 0);
         if (p_.order == SGFIM_ORDER_LEARNED) {
-            score(wfeat, kids.size(), wscore);
+            timed(4, [&] { score(wfeat, kids.size(), wscore); });
             for (size_t k = 0; k < kids.size(); ++k) defer[k] = wscore[k] < kDeferBelow;
         }
         // child masks for the children searched next: mask(child) = mask(parent) & row(e)
@@ -597,7 +604,7 @@ int Miner::finish(sgfim_result **out) {
                 qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
                 w0.push_back(ccheck_[c] / 64);
             }
-            run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_ANY2, cnt, w0.data());
+            timed(3, [&] { run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_ANY2, cnt, w0.data()); });
             for (uint64_t c = a; c < b; ++c) keep[c] = cnt[c - a] <= 1;
         }
     }
@@ -676,6 +683,8 @@ int Miner::finish(sgfim_result **out) {
     r->waves = waves_;
     r->kernel_launches = launches_;
     r->candidates = n;
+    phase_[5] = r->elapsed_s - (phase_[0] + phase_[1] + phase_[2] + phase_[3] + phase_[4]);
+    for (int i = 0; i < 6; ++i) r->phase_s[i] = phase_[i];
     *out = r;
     return SGFIM_OK;
 }

@@ -45,7 +45,7 @@ class Result(C.Structure):
                 ("elapsed_s", C.c_double), ("preprocess_s", C.c_double), ("nodes", C.c_uint64),
                 ("waves", C.c_uint64), ("kernel_launches", C.c_uint64), ("candidates", C.c_uint64),
                 ("trace_n", C.c_uint64), ("trace_dim", C.c_uint32), ("trace_features", f32p),
-                ("trace_labels", C.POINTER(C.c_uint8))]
+                ("trace_labels", C.POINTER(C.c_uint8)), ("phase_s", C.c_double * 6)]
 
 
 class MineParams(C.Structure):
@@ -67,7 +67,7 @@ class PhaseStats(C.Structure):
                 ("count_ms", C.c_double), ("tail_ms", C.c_double)]
 
 
-F_VERBOSE, F_IGNORE_ID0, F_PHASE_TIMERS = 0x1, 0x2, 0x4
+F_VERBOSE, F_IGNORE_ID0, F_PHASE_TIMERS, F_BLOCKING_SYNC = 0x1, 0x2, 0x4, 0x8
 
 
 class TfMeta(C.Structure):

@@ -96,7 +96,7 @@ def main(argv=None):
     report = {"workload": "anytime-2m", "n_txn": a.n_txn, "items": WORKLOAD["n_sensors"] * WORKLOAD["n_bins"],
               "floor": a.floor, "min_count": thr, "order": a.order, "mfis": len(res), "nodes": res.nodes,
               "waves": res.waves, "candidates": res.candidates, "kernel_launches": res.kernel_launches,
-              "mine_s": res.elapsed_s, "load_s": t_load, "gen_s": t_gen,
+              "mine_s": res.elapsed_s, "load_s": t_load, "gen_s": t_gen, "phase_s": res.phase_s,
               "time_to": {f"{int(f * 100)}%": res.time_to_coverage(f) for f in (0.5, 0.9, 0.95, 1.0)},
               "checkpoints": curve}
     if not a.no_verify:

@@ -45,6 +45,8 @@ class MineResult:
         self.waves = int(r.waves)
         self.kernel_launches = int(r.kernel_launches)
         self.candidates = int(r.candidates)
+        self.phase_s = dict(zip(("counts", "pool", "fhut", "final_filter", "scoring", "other"),
+                                (float(x) for x in r.phase_s)))
         tn, td = int(r.trace_n), int(r.trace_dim)
         if tn:
             self.trace_features = np.ctypeslib.as_array(r.trace_features, shape=(tn * td,)).reshape(tn, td).copy()
@@ -79,10 +81,10 @@ class MineResult:
 
 class Engine:
     def __init__(self, device=0, hbm_budget=0, wave_nodes=0, verbose=False, phase_timers=False,
-                 ignore_id0=False):
+                 ignore_id0=False, blocking_sync=False):
         self._L = L.load()
         flags = (L.F_VERBOSE if verbose else 0) | (L.F_PHASE_TIMERS if phase_timers else 0) | \
-            (L.F_IGNORE_ID0 if ignore_id0 else 0)
+            (L.F_IGNORE_ID0 if ignore_id0 else 0) | (L.F_BLOCKING_SYNC if blocking_sync else 0)
         cfg = L.Config(device, hbm_budget, wave_nodes, flags, None)
         h = C.c_void_p()
         rc = self._L.sgfim_open(C.byref(cfg), C.byref(h))

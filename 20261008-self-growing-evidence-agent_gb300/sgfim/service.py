@@ -29,7 +29,7 @@ from . import datagen
 from .engine import Engine, SgfimError
 
 WORKLOAD = dict(n_req=4096, len_lo=512, len_hi=65536, n_sensors=21, n_bins=6, n_regimes=8, alpha_bin=0.3,
-                floor_frac=0.02, rate_hz=2000.0, stream_rate=100_000.0, ring_txn=1 << 17)
+                floor_frac=0.02, rate_hz=2000.0, stream_rate=100_000.0, ring_txn=1 << 22)
 
 
 class Ring:
@@ -80,6 +80,8 @@ class Request:
     start_s: float = field(compare=False, default=0.0)
     done_s: float = field(compare=False, default=0.0)
     n_mfis: int = field(compare=False, default=0)
+    mine_s: float = field(compare=False, default=0.0)
+    nodes: int = field(compare=False, default=0)
     error: str = field(compare=False, default="")
     result: object = field(compare=False, default=None)
 
@@ -103,7 +105,7 @@ class WindowService:
     def __init__(self, workers=8, hbm_budget=8 << 30, device=0, ring_txn=WORKLOAD["ring_txn"], n_items=126,
                  keep_results=False):
         self.ring = Ring(n_items, ring_txn, device)
-        self.engines = [Engine(device=device) for _ in range(workers)]
+        self.engines = [Engine(device=device, blocking_sync=True) for _ in range(workers)]
         self.budget = hbm_budget
         self.n_items = n_items
         self.keep = keep_results
@@ -186,6 +188,8 @@ class WindowService:
                     thr = max(1, int(np.ceil(floor_frac * length)))
                     res = eng.mine(thr)
                     rq.n_mfis = len(res)
+                    rq.mine_s = res.elapsed_s
+                    rq.nodes = res.nodes
                     if self.keep:
                         rq.result = res.as_dict()
                 except SgfimError as e:
@@ -208,7 +212,12 @@ class WindowService:
         lat = np.array([r.done_s - r.arrival for r in done])
         errors = [r for r in done if r.error]
         first, last = min(r.arrival for r in requests), max(r.done_s for r in done)
+        mine = np.array([r.mine_s for r in done if not r.error] or [0.0])
+        queue = np.array([r.start_s - r.arrival for r in done])
         return {"windows": len(done), "errors": len(errors), "wall_s": wall,
+                "mine_ms_p50": float(np.percentile(mine, 50) * 1e3), "mine_ms_p99": float(np.percentile(mine, 99) * 1e3),
+                "mine_s_total": float(mine.sum()), "queue_ms_p50": float(np.percentile(queue, 50) * 1e3),
+                "nodes_total": int(sum(r.nodes for r in done)),
                 "windows_per_s": len(done) / max(last - first, 1e-9),
                 "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "mean_ms": float(lat.mean() * 1e3), "max_ms": float(lat.max() * 1e3),

@@ -64,6 +64,8 @@ typedef struct {
                                    use id 0 as a candidate (kernel_bitmap.cu:354-356,
                                    AnytimeMining/kernel.cu:338-341) */
 #define SGFIM_F_PHASE_TIMERS 0x4u /* record per-kernel CUDA events in support-batch calls */
+#define SGFIM_F_BLOCKING_SYNC 0x8u /* the miner waits for the device by sleeping, not spinning
+                                      (many concurrent handles on few host cores) */
 
 /* Open a handle on a device.  Replaces the engines' process start-up
  * (kernel_bitmap.cu:796-800, AnytimeMining/kernel.cu:798-805). */
@@ -215,6 +217,11 @@ typedef struct {
     uint32_t trace_dim;
     float *trace_features;   /* trace_n * trace_dim */
     uint8_t *trace_labels;   /* trace_n */
+    /* wall time of the search phases (each device phase ends in a stream
+     * synchronisation, so device time of asynchronous launches is charged to
+     * the next phase): [0] extension counts, [1] pool (HUT / leaf) queries,
+     * [2] FHUT counts, [3] final maximality filter, [4] scoring, [5] the rest */
+    double phase_s[6];
 } sgfim_result;
 
 #define SGFIM_TRACE_DIM 8

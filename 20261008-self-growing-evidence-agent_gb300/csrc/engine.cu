@@ -153,6 +153,7 @@ void sgfim_close(sgfim_handle *h) {
     h->dev_err.release();
     h->cooc_scratch.release();
     h->mws.release();
+    h->wws.release();
     h->scorer.w1.release(); h->scorer.b1.release(); h->scorer.w2.release();
     h->scorer.b2.release(); h->scorer.w3.release(); h->scorer.b3.release();
     for (auto &q : h->timer_busy)
@@ -178,7 +179,7 @@ namespace {
 int load_rows(sgfim_handle *h, const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn,
               const std::string &source) {
     Dataset &ds = h->ds;
-    ds = Dataset{};
+    reset_dataset(ds);
     ds.source = source;
     const uint64_t n_items = n_txn ? row_ptr[n_txn] : 0;
     uint32_t max_id = 0;
@@ -285,7 +286,7 @@ int sgfim_load_bitmaps(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uin
     API_GUARD_BEGIN
     cudaSetDevice(h->device);
     Dataset &ds = h->ds;
-    ds = Dataset{};
+    reset_dataset(ds);
     ds.source = "<bitmaps>";
     ds.n_txn = n_txn;
     ds.n_ids = d;

@@ -56,22 +56,73 @@ struct Dataset {
     std::string source;          // file name or "<memory>"
 };
 
+// Forget a dataset's contents but keep its device buffers for the next load
+// (DevBuf has no destructor: assigning a fresh Dataset would leak them).
+inline void reset_dataset(Dataset &ds) {
+    const DevBuf bm = ds.bitmaps, remap = ds.remap, sup = ds.sup_dev;
+    ds = Dataset{};
+    ds.bitmaps = bm;
+    ds.remap = remap;
+    ds.sup_dev = sup;
+}
+
 // A device copy staged through a pinned host buffer (both grow, never shrink).
+// The pinned buffer is written again only after the previous copy out of it
+// has executed (an event recorded behind each copy): a caller that puts twice
+// without synchronising the stream in between would otherwise overwrite bytes
+// the DMA engine has not read yet.
 struct Staged {
     DevBuf dev;
     HostBuf host;
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
     template <class T> T *put(const T *src, size_t n, cudaStream_t st) {
         const size_t b = (n ? n : 1) * sizeof(T);
+        if (pending) {
+            cudaError_t e = cudaEventSynchronize(ev);
+            if (e != cudaSuccess) throw CudaError(e, "cudaEventSynchronize", __FILE__, __LINE__);
+            pending = false;
+        }
         host.reserve(b);
         dev.reserve(b, st);
         if (n) {
             memcpy(host.ptr, src, n * sizeof(T));
             cudaError_t e = cudaMemcpyAsync(dev.ptr, host.ptr, n * sizeof(T), cudaMemcpyHostToDevice, st);
             if (e != cudaSuccess) throw CudaError(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+            if (!ev) {
+                e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+                if (e != cudaSuccess) throw CudaError(e, "cudaEventCreateWithFlags", __FILE__, __LINE__);
+            }
+            e = cudaEventRecord(ev, st);
+            if (e != cudaSuccess) throw CudaError(e, "cudaEventRecord", __FILE__, __LINE__);
+            pending = true;
         }
         return dev.template as<T>();
     }
-    void release() { dev.release(); host.release(); }
+    void release() {
+        if (ev) {
+            if (pending) cudaEventSynchronize(ev);
+            cudaEventDestroy(ev);
+        }
+        ev = nullptr;
+        pending = false;
+        dev.release();
+        host.release();
+    }
+};
+
+// Buffers of the batched window miner (sgfim_ring_mine_windows), kept by the
+// handle across calls: per-warp workspaces, the output arena, the window
+// table and its per-window results.
+struct WindowWorkspace {
+    DevBuf lists, lmfi, pool_m, pool_s, levels, out_m, out_s, ctrl, table, res;
+    HostBuf h_table, h_res, h_out;
+    void release() {
+        for (DevBuf *b : {&lists, &lmfi, &pool_m, &pool_s, &levels, &out_m, &out_s, &ctrl, &table, &res}) b->release();
+        h_table.release();
+        h_res.release();
+        h_out.release();
+    }
 };
 
 // Device and pinned buffers of the miner, kept by the handle across calls so
@@ -112,6 +163,7 @@ struct sgfim_handle {
     sg::DevBuf support_scratch, cand_ptr_dev, cand_items_dev, out_dev, dev_err;
     sg::DevBuf cooc_scratch;
     sg::MinerWorkspace mws;
+    sg::WindowWorkspace wws;
     sg::SupportPlan plan;
     uint64_t launches = 0;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;

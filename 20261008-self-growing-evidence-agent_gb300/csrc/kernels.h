@@ -98,4 +98,40 @@ int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64
                    cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches);
 size_t cooc_scratch_bytes(uint32_t d, uint64_t n_words, int kind);
 
+// Batched window miner (kernels_wmine.cu): one warp per window, windows taken
+// from `order` through the atomic counter `next`.  Per-warp workspaces are
+// laid out warp-major: lists list_cap x MW words, lmfi lmfi_cap, pool
+// pool_cap x MW words + pool_cap supports, levels wmine_level_bytes(MW).
+// win_status: 0 done, 1 workspace overflow (mine elsewhere), 2 output full.
+struct WMineParams {
+    const uint64_t *hm = nullptr;   // ring horizontal masks [capacity][MW]
+    uint64_t cap_mask = 0;          // ring capacity (transactions, power of two) - 1
+    uint32_t d = 0;
+    const uint64_t *starts = nullptr;
+    const uint32_t *lens = nullptr;
+    const uint32_t *thrs = nullptr;
+    const uint32_t *order = nullptr;
+    uint32_t n_win = 0;
+    uint32_t *next = nullptr;
+    uint64_t *lists = nullptr;
+    uint32_t list_cap = 0;
+    uint32_t *lmfi = nullptr;
+    uint32_t lmfi_cap = 0;
+    uint64_t *pool_m = nullptr;
+    uint32_t *pool_s = nullptr;
+    uint32_t pool_cap = 0;
+    void *levels = nullptr;
+    uint64_t *out_m = nullptr;
+    uint32_t *out_s = nullptr;
+    unsigned long long *out_pos = nullptr;
+    uint64_t out_cap = 0;
+    uint64_t *win_off = nullptr;
+    uint32_t *win_cnt = nullptr;
+    int32_t *win_status = nullptr;
+    uint64_t *win_nodes = nullptr;
+};
+size_t wmine_level_bytes(int mw);
+// blocks of 128 threads (4 warps)
+void launch_wmine(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
+
 }  // namespace sg

@@ -70,6 +70,13 @@ class PhaseStats(C.Structure):
 F_VERBOSE, F_IGNORE_ID0, F_PHASE_TIMERS, F_BLOCKING_SYNC = 0x1, 0x2, 0x4, 0x8
 
 
+class WindowsResult(C.Structure):
+    _fields_ = [("n_windows", C.c_uint64), ("mask_words", C.c_uint32), ("offset", u64p), ("masks", u64p),
+                ("support", u32p), ("status", C.POINTER(C.c_int32)), ("nodes", u64p),
+                ("batched", C.POINTER(C.c_uint8)), ("elapsed_s", C.c_double), ("kernel_ms", C.c_double),
+                ("launches", C.c_uint32)]
+
+
 class TfMeta(C.Structure):
     _fields_ = [("trans_set_file", C.c_char_p), ("support_threshold", C.c_double),
                 ("computation_time_s", C.c_double), ("preprocessing_time_s", C.c_double),
@@ -104,6 +111,9 @@ SIGNATURES = {
     "sgfim_ring_capacity": (C.c_uint64, [C.c_void_p]),
     "sgfim_ring_append": (C.c_int, [C.c_void_p, u64p, u32p, C.c_uint64]),
     "sgfim_ring_window_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]),
+    "sgfim_ring_mine_windows": (C.c_int, [C.c_void_p, C.c_void_p, u64p, u64p, u32p, C.c_uint64,
+                                          C.POINTER(C.POINTER(WindowsResult))]),
+    "sgfim_windows_result_free": (None, [C.POINTER(WindowsResult)]),
     "sgfim_support_batch_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
                                               C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),

@@ -65,10 +65,74 @@ class Ring:
         rc = self._L.sgfim_ring_window_load(self._r, eng.handle, int(start), int(length))
         eng._check(rc)
 
+    def mine_windows(self, eng, starts, lens, min_counts):
+        """MFIs of many windows in one batched launch (sgfim_ring_mine_windows)."""
+        starts = np.ascontiguousarray(starts, np.uint64)
+        lens = np.ascontiguousarray(lens, np.uint64)
+        mc = np.ascontiguousarray(min_counts, np.uint32)
+        n = len(starts)
+        if not (len(lens) == n and len(mc) == n):
+            raise ValueError("starts, lens and min_counts must have the same length")
+        if n == 0:
+            starts, lens, mc = np.zeros(1, np.uint64), np.zeros(1, np.uint64), np.zeros(1, np.uint32)
+        res = C.POINTER(L.WindowsResult)()
+        rc = self._L.sgfim_ring_mine_windows(self._r, eng.handle, starts.ctypes.data_as(L.u64p),
+                                             lens.ctypes.data_as(L.u64p), mc.ctypes.data_as(L.u32p), n,
+                                             C.byref(res))
+        eng._check(rc)
+        try:
+            return WindowsMined(res)
+        finally:
+            self._L.sgfim_windows_result_free(res)
+
     def close(self):
         if getattr(self, "_r", None):
             self._L.sgfim_ring_close(self._r)
             self._r = None
+
+
+def masks_to_sets(masks):
+    """[k, words] uint64 item masks -> list of ascending item-id tuples."""
+    masks = np.ascontiguousarray(masks, np.uint64)
+    if len(masks) == 0:
+        return []
+    bits = np.unpackbits(masks.view(np.uint8).reshape(len(masks), -1), axis=1, bitorder="little")
+    rows, cols = np.nonzero(bits)
+    cuts = np.searchsorted(rows, np.arange(1, len(masks)))
+    return [tuple(int(x) for x in c) for c in np.split(cols, cuts)]
+
+
+class WindowsMined:
+    """Per-window MFIs of sgfim_ring_mine_windows as numpy arrays."""
+
+    def __init__(self, res_ptr):
+        r = res_ptr.contents
+        n = int(r.n_windows)
+        self.mask_words = int(r.mask_words)
+        self.offset = np.ctypeslib.as_array(r.offset, shape=(n + 1,)).copy()
+        tot = int(self.offset[-1])
+        self.masks = (np.ctypeslib.as_array(r.masks, shape=(tot * self.mask_words,)).reshape(tot, self.mask_words).copy()
+                      if tot else np.zeros((0, self.mask_words), np.uint64))
+        self.support = np.ctypeslib.as_array(r.support, shape=(tot,)).copy() if tot else np.zeros(0, np.uint32)
+        self.status = np.ctypeslib.as_array(r.status, shape=(n,)).copy() if n else np.zeros(0, np.int32)
+        self.nodes = np.ctypeslib.as_array(r.nodes, shape=(n,)).copy() if n else np.zeros(0, np.uint64)
+        self.batched = np.ctypeslib.as_array(r.batched, shape=(n,)).copy() if n else np.zeros(0, np.uint8)
+        self.elapsed_s = float(r.elapsed_s)
+        self.kernel_ms = float(r.kernel_ms)
+        self.launches = int(r.launches)
+
+    def __len__(self):
+        return len(self.status)
+
+    def count(self, w):
+        return int(self.offset[w + 1] - self.offset[w])
+
+    def sets(self, w):
+        a, b = int(self.offset[w]), int(self.offset[w + 1])
+        return list(zip(masks_to_sets(self.masks[a:b]), (int(x) for x in self.support[a:b])))
+
+    def as_dict(self, w):
+        return {frozenset(s): c for s, c in self.sets(w)}
 
 
 @dataclass(order=True)
@@ -101,11 +165,40 @@ def window_bytes(length, n_items=126):
     return (n_items + slots) * words * 8 + n_items * 1026 * 8
 
 
+class WindowView:
+    """One window of a WindowsMined batch, with the MineResult accessors."""
+
+    def __init__(self, batch, w):
+        self.batch, self.w = batch, w
+
+    def __len__(self):
+        return self.batch.count(self.w)
+
+    def sets(self):
+        return self.batch.sets(self.w)
+
+    def as_dict(self):
+        return self.batch.as_dict(self.w)
+
+
 class WindowService:
+    """mode "batched": one scheduler thread hands every queued request to one
+    sgfim_ring_mine_windows launch (one warp per window; the handle's HBM
+    budget bounds the per-warp workspaces and the output arena).  mode
+    "workers": `workers` threads, each with its own handle, mine one window at
+    a time with the wave miner, admitted by a per-window memory estimate."""
+
     def __init__(self, workers=8, hbm_budget=8 << 30, device=0, ring_txn=WORKLOAD["ring_txn"], n_items=126,
-                 keep_results=False):
+                 keep_results=False, mode="batched", max_batch=8192):
+        if mode not in ("batched", "workers"):
+            raise ValueError("mode must be 'batched' or 'workers'")
+        self.mode = mode
+        self.max_batch = max_batch
         self.ring = Ring(n_items, ring_txn, device)
-        self.engines = [Engine(device=device, blocking_sync=True) for _ in range(workers)]
+        if mode == "batched":
+            self.engines = [Engine(device=device, hbm_budget=hbm_budget, blocking_sync=True)]
+        else:
+            self.engines = [Engine(device=device, blocking_sync=True) for _ in range(workers)]
         self.budget = hbm_budget
         self.n_items = n_items
         self.keep = keep_results
@@ -191,7 +284,7 @@ class WindowService:
                     rq.mine_s = res.elapsed_s
                     rq.nodes = res.nodes
                     if self.keep:
-                        rq.result = res.as_dict()
+                        rq.result = res   # numpy arrays; converted to Python sets after the run
                 except SgfimError as e:
                     rq.error = str(e)
                 finally:
@@ -200,7 +293,45 @@ class WindowService:
                 with lock:
                     done.append(rq)
 
-        threads = [threading.Thread(target=worker, args=(e,), daemon=True) for e in self.engines]
+        batches = []
+
+        def scheduler(eng):
+            while True:
+                with self._cv:
+                    while not work and not stop.is_set():
+                        self._cv.wait()
+                    if not work:
+                        return
+                    batch = [heapq.heappop(work) for _ in range(min(len(work), self.max_batch))]
+                t_start = time.perf_counter() - t0
+                lens = [min(rq.length, rq.end) for rq in batch]
+                starts = [rq.end - L_ for rq, L_ in zip(batch, lens)]
+                thrs = [max(1, int(np.ceil(floor_frac * L_))) for L_ in lens]
+                for rq in batch:
+                    rq.start_s = t_start
+                try:
+                    res = self.ring.mine_windows(eng, starts, lens, thrs)
+                    for i, rq in enumerate(batch):
+                        rq.n_mfis = res.count(i)
+                        rq.nodes = int(res.nodes[i])
+                        rq.mine_s = res.elapsed_s
+                        if res.status[i] != 0:
+                            rq.error = f"sgfim error {int(res.status[i])}"
+                        elif self.keep:
+                            rq.result = WindowView(res, i)
+                    batches.append({"windows": len(batch), "kernel_ms": res.kernel_ms, "call_s": res.elapsed_s,
+                                    "batched": int(res.batched.sum()), "launches": res.launches})
+                except SgfimError as e:
+                    for rq in batch:
+                        rq.error = str(e)
+                t_done = time.perf_counter() - t0
+                for rq in batch:
+                    rq.done_s = t_done
+                with lock:
+                    done.extend(batch)
+
+        target = scheduler if self.mode == "batched" else worker
+        threads = [threading.Thread(target=target, args=(e,), daemon=True) for e in self.engines]
         for t in threads:
             t.start()
         disp = threading.Thread(target=dispatcher, daemon=True)
@@ -214,7 +345,13 @@ class WindowService:
         first, last = min(r.arrival for r in requests), max(r.done_s for r in done)
         mine = np.array([r.mine_s for r in done if not r.error] or [0.0])
         queue = np.array([r.start_s - r.arrival for r in done])
-        return {"windows": len(done), "errors": len(errors), "wall_s": wall,
+        extra = {}
+        if batches:
+            extra = {"batches": len(batches), "batch_windows_mean": float(np.mean([b["windows"] for b in batches])),
+                     "kernel_ms_total": float(sum(b["kernel_ms"] for b in batches)),
+                     "call_s_total": float(sum(b["call_s"] for b in batches)),
+                     "batched_windows": int(sum(b["batched"] for b in batches))}
+        return {"mode": self.mode, **extra, "windows": len(done), "errors": len(errors), "wall_s": wall,
                 "mine_ms_p50": float(np.percentile(mine, 50) * 1e3), "mine_ms_p99": float(np.percentile(mine, 99) * 1e3),
                 "mine_s_total": float(mine.sum()), "queue_ms_p50": float(np.percentile(queue, 50) * 1e3),
                 "nodes_total": int(sum(r.nodes for r in done)),
@@ -276,6 +413,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description="sliding-window MFI service, workload windows-4096")
     ap.add_argument("--requests", type=int, default=WORKLOAD["n_req"])
     ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--mode", choices=("batched", "workers"), default="batched")
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     ap.add_argument("--check", action="store_true", help="compare every window with the oracle")
     ap.add_argument("--check-budget-s", type=float, default=240.0)
@@ -285,7 +423,7 @@ def main(argv=None):
     rows = stream_rows_for(a.requests)
     reqs = make_requests(a.requests, WORKLOAD["rate_hz"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
     svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
-                        keep_results=a.check)
+                        keep_results=a.check, mode=a.mode)
     # warm-up pass on a handful of requests (first-use allocations of every worker)
     warm = make_requests(2 * a.workers, 4000.0, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=99)
     svc.run(rows, warm, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
@@ -298,7 +436,8 @@ def main(argv=None):
     for rq in done:
         if rq.error:
             errs[rq.error] = errs.get(rq.error, 0) + 1
-    report = {"workload": "windows-4096", "requests": a.requests, "workers": a.workers,
+    report = {"workload": "windows-4096", "requests": a.requests,
+              "workers": a.workers if a.mode == "workers" else 1,
               "hbm_budget_gb": a.hbm_budget_gb, **rep, "error_kinds": errs,
               "config": {k: WORKLOAD[k] for k in WORKLOAD}}
     ctx = mp.get_context("spawn")
@@ -314,7 +453,7 @@ def main(argv=None):
             for rq, ref in zip(done, pool.imap(_check_window, jobs, chunksize=4)):
                 if rq.result is None:   # the request failed; counted in "errors"
                     continue
-                got = sorted((tuple(sorted(s)), c) for s, c in rq.result.items())
+                got = sorted((tuple(sorted(s)), c) for s, c in rq.result.sets())
                 checked += 1
                 mism += got != ref
                 if time.perf_counter() - t0 > a.check_budget_s:

@@ -325,6 +325,33 @@ int sgfim_ring_append(sgfim_ring *r, const uint64_t *row_ptr, const uint32_t *it
  * in the ring: head - start <= capacity and start + len <= head. */
 int sgfim_ring_window_load(sgfim_ring *r, sgfim_handle *h, uint64_t start, uint64_t len);
 
+/* MFIs of many windows of the ring in one persistent launch (no reference
+ * counterpart: the reference runs one engine process per window file).
+ * Window w is [starts[w], starts[w] + lens[w]) at absolute floor
+ * min_counts[w] (0 is taken as 1); its result equals sgfim_mine on
+ * sgfim_ring_window_load of the same window.  One warp mines one window
+ * (rings of at most 128 items); a window that outgrows the warp's workspace,
+ * or any window of a wider ring, is mined by the wave miner on `h` instead,
+ * so `h`'s dataset is replaced.  Appends from other threads may proceed
+ * meanwhile; an append that would overwrite a window still being mined waits
+ * for it. */
+typedef struct sgfim_windows_result {
+    uint64_t n_windows;
+    uint32_t mask_words;   /* 64-bit words per itemset mask; bit e = item e */
+    uint64_t *offset;      /* n_windows + 1: window w's MFIs are [offset[w], offset[w+1]) */
+    uint64_t *masks;       /* offset[n_windows] * mask_words words */
+    uint32_t *support;     /* offset[n_windows] */
+    int32_t *status;       /* per window, SGFIM_OK or the wave miner's error */
+    uint64_t *nodes;       /* search-tree nodes per window */
+    uint8_t *batched;      /* 1 = mined by the batched kernel, 0 = by the wave miner */
+    double elapsed_s;      /* whole call */
+    double kernel_ms;      /* batched kernel(s), device time */
+    uint32_t launches;     /* batched kernel launches */
+} sgfim_windows_result;
+int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *starts, const uint64_t *lens,
+                            const uint32_t *min_counts, uint64_t n_windows, sgfim_windows_result **out);
+void sgfim_windows_result_free(sgfim_windows_result *res);
+
 /* ---------------------------------------------------------------- scoring */
 
 /* Load the frontier-scoring MLP used by SGFIM_ORDER_LEARNED: 3 layers,

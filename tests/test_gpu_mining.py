@@ -170,3 +170,26 @@ def test_cli_shims_through_adapter(tmp_path):
     assert {k: dict(v) for k, v in a["stages"].items()} == want
     assert len(a["meta"]["runtimePerStage(s)"]) == 12
     assert a["meta"]["MFIsNumPerStage"] == [len(want[k]) for k in range(1, 13)]
+
+
+@pytest.mark.parametrize("wave_nodes,floor", [(1, 0.08), (7, 0.05), (64, 0.02), (0, 0.02)])
+def test_mine_exact_under_mask_arena_pressure(wave_nodes, floor):
+    """A 1 MiB budget leaves the miner ~100 tidset-mask slots, so most nodes
+    run without a mask (head-row queries) and masks are rebuilt at every wave
+    start; small waves stage many copies back to back.  Results must equal the
+    oracle's on window-shaped data at several seeds."""
+    from sgfim.engine import Engine
+    eng = Engine(hbm_budget=1 << 20, wave_nodes=wave_nodes)
+    try:
+        for seed in range(3):
+            n = 20_000 + 3_331 * seed
+            rows = datagen.regime_txns(n, 21, 6, 8, 0.3, seed=40 + seed)
+            rp, it = datagen.txns_to_csr(rows)
+            eng.load_csr(rp, it)
+            thr = int(np.ceil(floor * n))
+            got = eng.mine(thr).as_dict()
+            bm, _ = oracle.build_bitmaps(rp, it, 126)
+            ref, _ = oracle.mine_fast(bm, n, thr)
+            assert got == {frozenset(s): c for s, c in ref}, (wave_nodes, seed)
+    finally:
+        eng.close()

@@ -55,17 +55,96 @@ def test_ring_windows_match_slices(engine):
         ring.close()
 
 
-def test_service_windows_exact():
+@pytest.mark.parametrize("mode", ["batched", "workers"])
+def test_service_windows_exact(mode):
     from sgfim.service import WindowService, make_requests
     rows = datagen.regime_txns(200_000, 21, 6, 8, 0.3, seed=7)
     reqs = make_requests(48, 400.0, 512, 8192, seed=3)
-    svc = WindowService(workers=4, hbm_budget=2 << 30, ring_txn=1 << 16, keep_results=True)
+    svc = WindowService(workers=4, hbm_budget=2 << 30, ring_txn=1 << 16, keep_results=True, mode=mode)
     try:
         rep = svc.run(rows, reqs, stream_rate=20_000.0, floor_frac=0.05, warm_txn=8192)
     finally:
         svc.close()
-    assert rep["windows"] == 48 and rep["errors"] == 0
+    assert rep["windows"] == 48 and rep["errors"] == 0 and rep["mode"] == mode
+    if mode == "batched":
+        assert rep["batched_windows"] == 48
     for rq in rep["requests"]:
         length = min(rq.length, rq.end)
         thr = max(1, int(np.ceil(0.05 * length)))
-        assert rq.result == _oracle_mfis(rows[rq.end - length:rq.end], thr), rq.idx
+        assert rq.result.as_dict() == _oracle_mfis(rows[rq.end - length:rq.end], thr), rq.idx
+
+
+def test_ring_mine_windows_batched(engine):
+    """One batched launch over windows of every size class, including the
+    empty window, floors above the window length and floor 1, with the ring
+    wrapped: each window's MFIs equal the oracle's, and the kernel (not the
+    wave miner) mined them."""
+    from sgfim.service import Ring
+    rows = datagen.regime_txns(300_000, 21, 6, 8, 0.3, seed=11)
+    rp, it = datagen.txns_to_csr(rows)
+    ring = Ring(126, 1 << 17)
+    try:
+        ring.append(rp, it)            # wraps: the ring keeps the newest 131,072
+        head = ring.head
+        rng = np.random.default_rng(5)
+        lens = [0, 1, 7, 64, 65, 512, 513, 4096, 20_000, 65_536, 100_000]
+        lens += [int(np.exp(rng.uniform(np.log(512), np.log(65536)))) for _ in range(40)]
+        starts, thrs = [], []
+        for i, L in enumerate(lens):
+            starts.append(head - L - int(rng.integers(0, (1 << 17) - L + 1)))
+            thrs.append(max(1, int(np.ceil(0.02 * L))))
+        thrs[1] = 1
+        thrs[3] = 1000          # above the window length
+        thrs[5] = 1             # every distinct maximal transaction
+        res = ring.mine_windows(engine, starts, lens, thrs)
+        assert len(res) == len(lens) and (res.status == 0).all()
+        assert res.batched.all() and res.launches >= 1 and res.kernel_ms > 0
+        for w, (s, L, thr) in enumerate(zip(starts, lens, thrs)):
+            assert res.as_dict(w) == _oracle_mfis(rows[s:s + L], thr), (w, s, L, thr)
+        # the same windows through the wave miner agree
+        for w in (4, 7, 9):
+            ring.window_load(engine, starts[w], lens[w])
+            assert engine.mine(thrs[w]).as_dict() == res.as_dict(w)
+        # a window no longer in the ring is refused
+        from sgfim.engine import SgfimError
+        with pytest.raises(SgfimError):
+            ring.mine_windows(engine, [0], [10], [1])
+    finally:
+        ring.close()
+
+
+def test_appends_wait_for_windows_being_mined(engine):
+    """Appends from another thread that would overwrite windows of a running
+    batch wait for it; every window still matches the oracle."""
+    import threading
+    import time
+    from sgfim.service import Ring
+    rows = datagen.regime_txns(400_000, 21, 6, 8, 0.3, seed=13)
+    rp, it = datagen.txns_to_csr(rows)
+    cap = 1 << 16
+    ring = Ring(126, cap)
+    try:
+        ring.append(rp[:cap + 1], it[:int(rp[cap])])
+        lens = [4096] * 24 + [cap - 100]
+        starts = [i * 2000 for i in range(24)] + [50]
+        thrs = [max(1, int(np.ceil(0.02 * L))) for L in lens]
+        out = {}
+
+        def miner():
+            out["res"] = ring.mine_windows(engine, starts, lens, thrs)
+
+        m = threading.Thread(target=miner)
+        m.start()
+        time.sleep(0.05)      # the call registers its windows first thing
+        # ten batches, the first of which already overwrites the oldest windows
+        for k in range(10):
+            a, b = cap + k * 10_000, cap + (k + 1) * 10_000
+            ring.append(rp[a:b + 1] - rp[a], it[int(rp[a]):int(rp[b])])
+        out["head"] = ring.head
+        m.join()
+        res = out["res"]
+        assert out["head"] == cap + 100_000 and (res.status == 0).all()
+        for w, (s, L, thr) in enumerate(zip(starts, lens, thrs)):
+            assert res.as_dict(w) == _oracle_mfis(rows[s:s + L], thr), w
+    finally:
+        ring.close()

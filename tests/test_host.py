@@ -162,3 +162,13 @@ def test_two_rank_sharded_supports_gloo(tmp_path):
     mp.start_processes(_shard_worker, args=(2, port, out), nprocs=2, start_method="spawn")
     ok, n = np.load(out)
     assert ok == 1 and n == 1001
+
+
+def test_masks_to_sets():
+    from sgfim.service import masks_to_sets
+    m = np.zeros((4, 2), np.uint64)
+    m[0, 0] = 0b1011
+    m[1, 1] = 1 << 63
+    m[2] = [1 << 63, 1]
+    assert masks_to_sets(m) == [(0, 1, 3), (127,), (63, 64), ()]
+    assert masks_to_sets(np.zeros((0, 2), np.uint64)) == []

@@ -81,18 +81,6 @@ cudaEvent_t *sgfim_handle::timer_quad() {
     return timer_busy.back().e;
 }
 
-#define API_GUARD_BEGIN try {
-#define API_GUARD_END(h)                                                   \
-    }                                                                      \
-    catch (const sg::CudaError &e) {                                       \
-        return sg::fail(h, SGFIM_EDEVICE, e.what);                         \
-    }                                                                      \
-    catch (const sg::EngineError &e) {                                     \
-        return sg::fail(h, e.code, e.what);                                \
-    }                                                                      \
-    catch (const std::bad_alloc &) {                                       \
-        return sg::fail(h, SGFIM_ENOMEM, "host allocation failed");        \
-    }
 
 extern "C" {
 

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -183,6 +184,21 @@ struct sgfim_handle {
     sgfim_phase_stats pstats{};
     cudaEvent_t *timer_quad();
 };
+
+// Body of an exported function: CUDA, engine and host-allocation failures
+// become return codes (no exception crosses the C ABI).
+#define API_GUARD_BEGIN try {
+#define API_GUARD_END(h)                                                   \
+    }                                                                      \
+    catch (const sg::CudaError &e) {                                       \
+        return sg::fail(h, SGFIM_EDEVICE, e.what);                         \
+    }                                                                      \
+    catch (const sg::EngineError &e) {                                     \
+        return sg::fail(h, e.code, e.what);                                \
+    }                                                                      \
+    catch (const std::bad_alloc &) {                                       \
+        return sg::fail(h, SGFIM_ENOMEM, "host allocation failed");        \
+    }
 
 namespace sg {
 int fail(sgfim_handle *h, int code, const std::string &msg);

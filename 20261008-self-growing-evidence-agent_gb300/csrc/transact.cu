@@ -1,0 +1,307 @@
+// transact.cu -- sensor stream -> transactions on the GPU.
+//
+// Reference: code/pipeline/skab_spike.py
+//   fit_bins            :38-52  per-sensor quantiles at linspace(0, 1, n_bins+1)
+//                               (numpy "linear" method), unique edges, a
+//                               constant column gets [e0 - 0.5, e0 + 0.5]
+//   bin_index           :55-58  searchsorted(edges, v, side="right") - 1, clamped
+//   window_transactions :62-80  windows s = 0, stride, ..., s + window <= n; the
+//                               median of each sensor over the window picks one
+//                               item per sensor; the label is the window's max
+// Items are dense ids sensor * n_bins + bin.
+//
+// Device work: the row-major [n, S] matrix is transposed to columns; every
+// order statistic numpy's quantile needs is found exactly by an 8-pass MSD
+// radix select over order-preserving 64-bit keys of the doubles (one CTA per
+// sensor x rank); the quantile interpolation runs in explicitly rounded
+// double intrinsics, so no multiply-add is fused and the edges are the same
+// doubles numpy computes; one thread per (window, sensor) sorts its window
+// and bins the median.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+
+namespace sg {
+
+namespace {
+
+constexpr uint32_t kMaxWindow = 256;
+
+__device__ __forceinline__ uint64_t dkey(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | (1ull << 63));
+}
+__device__ __forceinline__ double dkey_inv(uint64_t k) {
+    const uint64_t b = (k >> 63) ? (k & ~(1ull << 63)) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void to_columns_kernel(const double *__restrict__ rows, uint64_t n, uint32_t S, double *__restrict__ cols,
+                                  uint32_t *__restrict__ nan_count) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n * S; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i / S;
+        const uint32_t c = (uint32_t)(i - r * S);
+        const double v = rows[i];
+        if (v != v) atomicAdd(nan_count, 1u);
+        cols[(uint64_t)c * n + r] = v;
+    }
+}
+
+// k-th smallest (0-based) of column blockIdx.y for rank ranks[blockIdx.y * R + blockIdx.x]
+__global__ void __launch_bounds__(512) kth_kernel(const double *__restrict__ cols, uint64_t n, const uint64_t *__restrict__ ranks,
+                                                  uint32_t R, double *__restrict__ out) {
+    __shared__ uint32_t hist[256];
+    __shared__ uint64_t s_prefix, s_mask, s_k;
+    const uint32_t s = blockIdx.y, r = blockIdx.x;
+    const double *col = cols + (uint64_t)s * n;
+    if (threadIdx.x == 0) {
+        s_prefix = 0;
+        s_mask = 0;
+        s_k = ranks[(uint64_t)s * R + r];
+    }
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 56 - 8 * pass;
+        for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const uint64_t prefix = s_prefix, mask = s_mask;
+        for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const uint64_t key = dkey(col[i]);
+            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t k = s_k, cum = 0;
+            uint32_t dgt = 255;
+            for (uint32_t d = 0; d < 256; ++d) {
+                if (k < cum + hist[d]) {
+                    dgt = d;
+                    break;
+                }
+                cum += hist[d];
+            }
+            s_prefix = prefix | ((uint64_t)dgt << shift);
+            s_mask = mask | (255ull << shift);
+            s_k = k - cum;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(uint64_t)s * R + r] = dkey_inv(s_prefix);
+}
+
+// numpy linear quantile for quantile q of sensor s: lo/hi are the order
+// statistics at floor(h) and floor(h)+1 (both the last one when h >= n-1),
+// gamma = h - floor(h) (h - (-1) above the bounds, where lo == hi), and
+// lerp(a, b, g) = g >= 0.5 ? b - (b - a) * (1 - g) : a + (b - a) * g.
+__global__ void quantile_kernel(const double *__restrict__ stats, uint32_t R, const uint32_t *__restrict__ lo_idx,
+                                const uint32_t *__restrict__ hi_idx, const double *__restrict__ gamma, uint32_t nq,
+                                uint32_t S, double *__restrict__ edges) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq * S) return;
+    const uint32_t s = i / nq, q = i - s * nq;
+    const double a = stats[(uint64_t)s * R + lo_idx[q]];
+    const double b = stats[(uint64_t)s * R + hi_idx[q]];
+    const double g = gamma[q];
+    const double diff = __dsub_rn(b, a);
+    double v = __dadd_rn(a, __dmul_rn(diff, g));
+    if (g >= 0.5) v = __dsub_rn(b, __dmul_rn(diff, __dsub_rn(1.0, g)));
+    edges[i] = v;
+}
+
+// One thread per (window, sensor): median of the window's values, binned.
+__global__ void window_bin_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t window,
+                                  uint32_t stride, uint64_t n_win, const double *__restrict__ edges,
+                                  const uint32_t *__restrict__ n_edges, uint32_t edge_stride, uint32_t n_bins,
+                                  const int32_t *__restrict__ anomaly, uint32_t *__restrict__ items,
+                                  int32_t *__restrict__ labels) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n_win * S) return;
+    const uint64_t w = i / S;
+    const uint32_t s = (uint32_t)(i - w * S);
+    const uint64_t start = w * stride;
+    const double *col = cols + (uint64_t)s * n + start;
+    double buf[kMaxWindow];
+    for (uint32_t j = 0; j < window; ++j) {
+        // insertion sort while loading
+        const double v = col[j];
+        uint32_t k = j;
+        while (k > 0 && buf[k - 1] > v) {
+            buf[k] = buf[k - 1];
+            --k;
+        }
+        buf[k] = v;
+    }
+    const double med = (window & 1) ? buf[window / 2] : __ddiv_rn(__dadd_rn(buf[window / 2 - 1], buf[window / 2]), 2.0);
+    const double *e = edges + (uint64_t)s * edge_stride;
+    const uint32_t m = n_edges[s];
+    uint32_t cnt = 0;   // edges <= med (searchsorted side="right")
+    for (uint32_t j = 0; j < m; ++j) cnt += e[j] <= med;
+    int32_t b = (int32_t)cnt - 1;
+    if (b < 0) b = 0;
+    if (b > (int32_t)m - 2) b = (int32_t)m - 2;
+    items[w * S + s] = s * n_bins + (uint32_t)b;
+    if (s == 0) {
+        int32_t mx = 0;
+        if (anomaly) {
+            mx = anomaly[start];
+            for (uint32_t j = 1; j < window; ++j) mx = max(mx, anomaly[start + j]);
+        }
+        labels[w] = mx;
+    }
+}
+
+}  // namespace
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sgfim_transactionize(sgfim_handle *h, const double *values, uint64_t n_rows, uint32_t n_sensors,
+                                    const int32_t *anomaly, uint32_t window, uint32_t stride, uint32_t n_bins,
+                                    uint32_t flags, double *edges_out, uint32_t *n_edges_out, uint32_t *items_out,
+                                    int32_t *labels_out, uint64_t *n_windows_out) {
+    if (!h) return SGFIM_EINVAL;
+    if (!values && n_rows) return fail(h, SGFIM_EINVAL, "null values");
+    if (n_sensors == 0 || n_bins < 1 || window < 1 || stride < 1)
+        return fail(h, SGFIM_EINVAL, "n_sensors, n_bins, window and stride must be >= 1");
+    if (window > kMaxWindow) return fail(h, SGFIM_EINVAL, "window longer than 256 rows");
+    if (n_rows == 0) return fail(h, SGFIM_EINVAL, "empty stream");
+    if ((uint64_t)n_sensors * n_bins > 0xffffffffull) return fail(h, SGFIM_EINVAL, "too many items");
+    const uint64_t n_win = n_rows >= window ? (n_rows - window) / stride + 1 : 0;
+    if (n_windows_out) *n_windows_out = n_win;
+    if (!edges_out || !n_edges_out || (n_win && (!items_out || !labels_out)))
+        return fail(h, SGFIM_EINVAL, "null output");
+    API_GUARD_BEGIN
+    SG_CUDA_TRY(cudaSetDevice(h->device));
+    cudaStream_t st = h->stream;
+    const uint32_t S = n_sensors, nq = n_bins + 1;
+    // quantile positions exactly as numpy computes them
+    std::vector<double> q(nq), gamma(nq);
+    const double step = 1.0 / (double)n_bins;
+    for (uint32_t i = 0; i < nq; ++i) q[i] = (double)i * step + 0.0;
+    q[nq - 1] = 1.0;
+    std::vector<uint64_t> need;   // order statistics
+    std::vector<uint32_t> lo_pos(nq), hi_pos(nq);
+    std::vector<uint64_t> lo_rank(nq), hi_rank(nq);
+    const double nm1 = (double)(n_rows - 1);
+    for (uint32_t i = 0; i < nq; ++i) {
+        volatile double h_ = nm1 * q[i];   // one rounding, as numpy's (n - 1) * quantiles
+        const double hv = h_;
+        double prev = std::floor(hv);
+        uint64_t lo, hi;
+        if (hv >= nm1) {
+            lo = hi = n_rows - 1;
+            prev = -1.0;
+        } else {
+            lo = (uint64_t)prev;
+            hi = lo + 1;
+        }
+        volatile double g_ = hv - prev;
+        gamma[i] = g_;
+        lo_rank[i] = lo;
+        hi_rank[i] = hi;
+        need.push_back(lo);
+        need.push_back(hi);
+    }
+    std::sort(need.begin(), need.end());
+    need.erase(std::unique(need.begin(), need.end()), need.end());
+    for (uint32_t i = 0; i < nq; ++i) {
+        lo_pos[i] = (uint32_t)(std::lower_bound(need.begin(), need.end(), lo_rank[i]) - need.begin());
+        hi_pos[i] = (uint32_t)(std::lower_bound(need.begin(), need.end(), hi_rank[i]) - need.begin());
+    }
+    const uint32_t R = (uint32_t)need.size();
+    std::vector<uint64_t> ranks((size_t)S * R);
+    for (uint32_t s = 0; s < S; ++s)
+        for (uint32_t r = 0; r < R; ++r) ranks[(size_t)s * R + r] = need[r];
+
+    DevBuf d_rows, d_cols, d_small, d_anom, d_items;
+    struct Free {
+        DevBuf *b[5];
+        ~Free() {
+            for (DevBuf *x : b) x->release();
+        }
+    } guard{{&d_rows, &d_cols, &d_small, &d_anom, &d_items}};
+    const size_t mat = (size_t)n_rows * S * 8;
+    d_rows.reserve(mat, st);
+    d_cols.reserve(mat, st);
+    // small buffers: nan count | ranks | stats | lo | hi | gamma | edges | n_edges | labels
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t o_nan = carve(4), o_rank = carve(ranks.size() * 8), o_stat = carve(ranks.size() * 8),
+                 o_lo = carve(nq * 4), o_hi = carve(nq * 4), o_g = carve(nq * 8), o_edge = carve((size_t)S * nq * 8),
+                 o_ne = carve((size_t)S * 4), o_lab = carve(std::max<uint64_t>(n_win, 1) * 4);
+    d_small.reserve(off, st);
+    char *base = d_small.as<char>();
+    SG_CUDA_TRY(cudaMemcpyAsync(d_rows.ptr, values, mat, cudaMemcpyHostToDevice, st));
+    SG_CUDA_TRY(cudaMemsetAsync(base + o_nan, 0, 4, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(base + o_rank, ranks.data(), ranks.size() * 8, cudaMemcpyHostToDevice, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(base + o_lo, lo_pos.data(), nq * 4, cudaMemcpyHostToDevice, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(base + o_hi, hi_pos.data(), nq * 4, cudaMemcpyHostToDevice, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(base + o_g, gamma.data(), nq * 8, cudaMemcpyHostToDevice, st));
+    const uint64_t total = n_rows * S;
+    to_columns_kernel<<<(unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)h->n_sm * 32), 256, 0, st>>>(
+        d_rows.as<double>(), n_rows, S, d_cols.as<double>(), reinterpret_cast<uint32_t *>(base + o_nan));
+    SG_CUDA_TRY(cudaGetLastError());
+    kth_kernel<<<dim3(R, S), 512, 0, st>>>(d_cols.as<double>(), n_rows, reinterpret_cast<const uint64_t *>(base + o_rank),
+                                           R, reinterpret_cast<double *>(base + o_stat));
+    SG_CUDA_TRY(cudaGetLastError());
+    quantile_kernel<<<(S * nq + 127) / 128, 128, 0, st>>>(
+        reinterpret_cast<const double *>(base + o_stat), R, reinterpret_cast<const uint32_t *>(base + o_lo),
+        reinterpret_cast<const uint32_t *>(base + o_hi), reinterpret_cast<const double *>(base + o_g), nq, S,
+        reinterpret_cast<double *>(base + o_edge));
+    SG_CUDA_TRY(cudaGetLastError());
+    h->launches += 3;
+    uint32_t nan_count = 0;
+    std::vector<double> raw((size_t)S * nq);
+    SG_CUDA_TRY(cudaMemcpyAsync(&nan_count, base + o_nan, 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaMemcpyAsync(raw.data(), base + o_edge, raw.size() * 8, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (nan_count) return fail(h, SGFIM_EINVAL, "the stream holds NaN values");
+    // np.unique of each sensor's quantiles (already ascending), constant column rule
+    std::vector<double> edges((size_t)S * nq, 0.0);
+    std::vector<uint32_t> n_edges(S);
+    for (uint32_t s = 0; s < S; ++s) {
+        std::vector<double> e(raw.begin() + (size_t)s * nq, raw.begin() + (size_t)(s + 1) * nq);
+        std::stable_sort(e.begin(), e.end());
+        std::vector<double> u;
+        for (double x : e)
+            if (u.empty() || !(x == u.back())) u.push_back(x);
+        if (u.size() < 2) u = {u[0] - 0.5, u[0] + 0.5};
+        n_edges[s] = (uint32_t)u.size();
+        std::copy(u.begin(), u.end(), edges.begin() + (size_t)s * nq);
+    }
+    memcpy(edges_out, edges.data(), edges.size() * 8);
+    memcpy(n_edges_out, n_edges.data(), (size_t)S * 4);
+    if (n_win) {
+        SG_CUDA_TRY(cudaMemcpyAsync(base + o_edge, edges.data(), edges.size() * 8, cudaMemcpyHostToDevice, st));
+        SG_CUDA_TRY(cudaMemcpyAsync(base + o_ne, n_edges.data(), (size_t)S * 4, cudaMemcpyHostToDevice, st));
+        if (anomaly) {
+            d_anom.reserve(n_rows * 4, st);
+            SG_CUDA_TRY(cudaMemcpyAsync(d_anom.ptr, anomaly, n_rows * 4, cudaMemcpyHostToDevice, st));
+        }
+        d_items.reserve(n_win * S * 4, st);
+        const uint64_t nt = n_win * S;
+        window_bin_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(
+            d_cols.as<double>(), n_rows, S, window, stride, n_win, reinterpret_cast<const double *>(base + o_edge),
+            reinterpret_cast<const uint32_t *>(base + o_ne), nq, n_bins, anomaly ? d_anom.as<int32_t>() : nullptr,
+            d_items.as<uint32_t>(), reinterpret_cast<int32_t *>(base + o_lab));
+        SG_CUDA_TRY(cudaGetLastError());
+        h->launches += 1;
+        SG_CUDA_TRY(cudaMemcpyAsync(items_out, d_items.ptr, nt * 4, cudaMemcpyDeviceToHost, st));
+        SG_CUDA_TRY(cudaMemcpyAsync(labels_out, base + o_lab, n_win * 4, cudaMemcpyDeviceToHost, st));
+        SG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    if (flags & SGFIM_TX_LOAD) {
+        std::vector<uint64_t> rp(n_win + 1);
+        for (uint64_t w = 0; w <= n_win; ++w) rp[w] = w * S;
+        return sgfim_load_csr(h, rp.data(), items_out, n_win);
+    }
+    return SGFIM_OK;
+    API_GUARD_END(h)
+}

@@ -68,6 +68,7 @@ class PhaseStats(C.Structure):
 
 
 F_VERBOSE, F_IGNORE_ID0, F_PHASE_TIMERS, F_BLOCKING_SYNC = 0x1, 0x2, 0x4, 0x8
+TX_LOAD = 0x1
 
 
 class WindowsResult(C.Structure):
@@ -114,6 +115,9 @@ SIGNATURES = {
     "sgfim_ring_mine_windows": (C.c_int, [C.c_void_p, C.c_void_p, u64p, u64p, u32p, C.c_uint64,
                                           C.POINTER(C.POINTER(WindowsResult))]),
     "sgfim_windows_result_free": (None, [C.POINTER(WindowsResult)]),
+    "sgfim_transactionize": (C.c_int, [C.c_void_p, f64p, C.c_uint64, C.c_uint32, C.POINTER(C.c_int32), C.c_uint32,
+                                       C.c_uint32, C.c_uint32, C.c_uint32, f64p, u32p, u32p, C.POINTER(C.c_int32),
+                                       u64p]),
     "sgfim_support_batch_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
                                               C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),

@@ -200,3 +200,26 @@ def write_fimi_ids(path, rows, one_based=True):
             for r in rows:
                 f.write(" ".join(str(x + off) for x in sorted(set(r))))
                 f.write("\n")
+
+
+def sensor_stream(n_rows, n_sensors, seed, constant_cols=(), anomaly_rate_permille=50):
+    """Seeded synthetic sensor stream in thousandths (ties, as in CSV input):
+    per-sensor integer random-walk level, regime shifts, a triangle wave and
+    noise, built from integer draws only so every platform produces the same
+    doubles; listed columns are constant.  Returns (values [n, S] float64,
+    anomaly [n] int32)."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(n_rows, dtype=np.int64)
+    vals = np.empty((n_rows, n_sensors), dtype=np.float64)
+    regime = np.cumsum(rng.integers(0, 500, n_rows) == 0) % 4
+    for c in range(n_sensors):
+        level = np.cumsum(rng.integers(-20, 21, n_rows))
+        shift = rng.integers(-1500, 1501, 4)[regime]
+        period = int(rng.integers(50, 400))
+        tri = np.abs((t % period) - period // 2) * 8
+        noise = rng.integers(-300, 301, n_rows)
+        vals[:, c] = (level + shift + tri + noise) / 1000.0
+    for c in constant_cols:
+        vals[:, c] = 1.25
+    anom = (rng.integers(0, 1000, n_rows) < anomaly_rate_permille).astype(np.int32)
+    return vals, anom

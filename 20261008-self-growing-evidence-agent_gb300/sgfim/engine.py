@@ -138,6 +138,36 @@ class Engine:
         from .datagen import txns_to_csr
         return self.load_csr(*txns_to_csr(rows))
 
+    def transactionize(self, values, window=30, stride=15, n_bins=3, anomaly=None, load=False):
+        """Sensor stream [n_rows, n_sensors] -> (items [n_windows, n_sensors]
+        dense ids, labels [n_windows], edges: list of per-sensor arrays) on the
+        GPU (sgfim_transactionize); ``load=True`` also makes the transactions
+        this handle's dataset."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        if values.ndim != 2:
+            raise ValueError("values must be [n_rows, n_sensors]")
+        n, S = values.shape
+        an = None
+        if anomaly is not None:
+            an = np.ascontiguousarray(anomaly, dtype=np.int32)
+            if an.shape != (n,):
+                raise ValueError("one anomaly flag per row")
+        n_win = (n - window) // stride + 1 if n >= window else 0
+        edges = np.zeros(S * (n_bins + 1), np.float64)
+        n_edges = np.zeros(S, np.uint32)
+        items = np.zeros(max(1, n_win * S), np.uint32)
+        labels = np.zeros(max(1, n_win), np.int32)
+        nw = C.c_uint64(0)
+        rc = self._L.sgfim_transactionize(self._h, _p(values, C.c_double), n, S,
+                                          an.ctypes.data_as(C.POINTER(C.c_int32)) if an is not None else None,
+                                          window, stride, n_bins, L.TX_LOAD if load else 0, _p(edges, C.c_double),
+                                          _p(n_edges, C.c_uint32), _p(items, C.c_uint32),
+                                          labels.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(nw))
+        self._check(rc)
+        assert nw.value == n_win
+        e = [edges[s * (n_bins + 1):s * (n_bins + 1) + int(n_edges[s])].copy() for s in range(S)]
+        return items[:n_win * S].reshape(n_win, S).astype(np.int64), labels[:n_win].astype(np.int64), e
+
     def load_bitmaps(self, bm, n_txn):
         bm = np.ascontiguousarray(bm, dtype=np.uint64)
         d, w = bm.shape

@@ -352,6 +352,26 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                             const uint32_t *min_counts, uint64_t n_windows, sgfim_windows_result **out);
 void sgfim_windows_result_free(sgfim_windows_result *res);
 
+/* ---------------------------------------------------------------- transactionisation */
+
+/* Sensor stream -> transactions on the GPU (code/pipeline/skab_spike.py:
+ * fit_bins :38-52, bin_index :55-58, window_transactions :62-80).  `values` is
+ * the row-major [n_rows, n_sensors] stream (NaN-free: EINVAL otherwise),
+ * `anomaly` (nullable) its per-row 0/1 flags.  Per sensor the bin edges are
+ * numpy's linear-method quantiles at linspace(0, 1, n_bins+1), made unique (a
+ * constant column gets [v-0.5, v+0.5]); written to edges_out[s*(n_bins+1) ..]
+ * with their count in n_edges_out[s].  Windows start at 0, stride, ... while
+ * start + window <= n_rows (n_windows = (n_rows - window) / stride + 1, or
+ * 0); window w's transaction is one item per sensor, s * n_bins + bin of the
+ * window median, in items_out[w * n_sensors + s]; labels_out[w] = max of the
+ * window's flags (0 without flags).  window <= 256.  With SGFIM_TX_LOAD the
+ * transactions also become the handle's dataset (as sgfim_load_csr). */
+#define SGFIM_TX_LOAD 0x1u
+int sgfim_transactionize(sgfim_handle *h, const double *values, uint64_t n_rows, uint32_t n_sensors,
+                         const int32_t *anomaly, uint32_t window, uint32_t stride, uint32_t n_bins, uint32_t flags,
+                         double *edges_out, uint32_t *n_edges_out, uint32_t *items_out, int32_t *labels_out,
+                         uint64_t *n_windows_out);
+
 /* ---------------------------------------------------------------- scoring */
 
 /* Load the frontier-scoring MLP used by SGFIM_ORDER_LEARNED: 3 layers,

@@ -172,3 +172,12 @@ def test_masks_to_sets():
     m[2] = [1 << 63, 1]
     assert masks_to_sets(m) == [(0, 1, 3), (127,), (63, 64), ()]
     assert masks_to_sets(np.zeros((0, 2), np.uint64)) == []
+
+
+def test_label_dataset_appends_one_label_per_row():
+    from sgfim.patterns import label_dataset
+    rows = [[0, 2], [], [1], [0, 1, 2]]
+    rp, it, a, n = label_dataset(rows, [1, 0, 0, 1])
+    assert (a, n) == (3, 4)
+    got = [list(it[int(rp[r]):int(rp[r + 1])]) for r in range(4)]
+    assert got == [[0, 2, 3], [4], [1, 4], [0, 1, 2, 3]]

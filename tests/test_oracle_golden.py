@@ -166,3 +166,22 @@ def test_tensorfim_strict_root_rule():
     assert got == {}
     got = oracle.tensorfim_mfis(rows, 0.35)  # thr 3.5 -> counts >= 4 frequent, roots count/n > .35
     assert got == {frozenset({1}): 4, frozenset({4}): 4}
+
+
+TX_GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "transact_golden.json")))["cases"]
+
+
+@pytest.mark.parametrize("case", TX_GOLD, ids=[f"seed{c['case']['seed']}" for c in TX_GOLD])
+def test_transact_oracle_matches_reference(case):
+    """The numpy restatement of fit_bins / window_transactions reproduces the
+    reference's own outputs (edges bit for bit, items, labels)."""
+    import hashlib
+    from oracle import transact
+    from sgfim import datagen
+    c = case["case"]
+    vals, anom = datagen.sensor_stream(c["n_rows"], c["n_sensors"], c["seed"], constant_cols=c["constant_cols"])
+    assert hashlib.sha256(np.ascontiguousarray(vals, dtype="<f8").tobytes()).hexdigest() == case["values_sha256"]
+    edges = transact.fit_bins(vals, c["n_bins"])
+    assert [[float(x).hex() for x in e] for e in edges] == case["edges"]
+    items, labels = transact.window_items(vals, edges, c["window"], c["stride"], anom, c["n_bins"])
+    assert items.tolist() == case["items"] and labels.tolist() == case["labels"]

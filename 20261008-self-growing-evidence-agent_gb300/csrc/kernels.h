@@ -98,21 +98,29 @@ int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64
                    cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches);
 size_t cooc_scratch_bytes(uint32_t d, uint64_t n_words, int kind);
 
-// Batched window miner (kernels_wmine.cu): one warp per window, windows taken
-// from `order` through the atomic counter `next`.  Per-warp workspaces are
-// laid out warp-major: lists list_cap x MW words, lmfi lmfi_cap, pool
-// pool_cap x MW words + pool_cap supports, levels wmine_level_bytes(MW).
-// win_status: 0 done, 1 workspace overflow (mine elsewhere), 2 output full.
+// Batched window miner (kernels_wmine.cu).  A task is a whole window
+// (child == kWholeWindow) or one subtree of a split window's root (child =
+// index into the root's sorted frequent tail; wroot_kernel fills the root
+// records first).  Per-warp workspaces are warp-major: lists list_cap x MW
+// words, lmfi lmfi_cap, pool pool_cap x MW words + pool_cap supports, levels
+// wmine_level_bytes(MW).  task_status: 0 done, 1 workspace overflow (mine the
+// window elsewhere), 2 output arena full (retry the task).
+constexpr uint32_t kWholeWindow = 0xffffffffu;
 struct WMineParams {
     const uint64_t *hm = nullptr;   // ring horizontal masks [capacity][MW]
     uint64_t cap_mask = 0;          // ring capacity (transactions, power of two) - 1
     uint32_t d = 0;
-    const uint64_t *starts = nullptr;
+    const uint64_t *starts = nullptr;   // per window
     const uint32_t *lens = nullptr;
     const uint32_t *thrs = nullptr;
-    const uint32_t *order = nullptr;
-    uint32_t n_win = 0;
-    uint32_t *next = nullptr;
+    void *roots = nullptr;              // per window, wmine_root_bytes(MW) each
+    const uint32_t *split_win = nullptr;
+    uint32_t n_split = 0;
+    const uint32_t *task_win = nullptr;
+    const uint32_t *task_child = nullptr;
+    const uint32_t *task_order = nullptr;
+    uint32_t n_tasks = 0;
+    uint32_t *next = nullptr;           // [0] task counter, [1] root counter
     uint64_t *lists = nullptr;
     uint32_t list_cap = 0;
     uint32_t *lmfi = nullptr;
@@ -125,13 +133,45 @@ struct WMineParams {
     uint32_t *out_s = nullptr;
     unsigned long long *out_pos = nullptr;
     uint64_t out_cap = 0;
-    uint64_t *win_off = nullptr;
-    uint32_t *win_cnt = nullptr;
-    int32_t *win_status = nullptr;
-    uint64_t *win_nodes = nullptr;
+    uint64_t *task_off = nullptr;
+    uint32_t *task_cnt = nullptr;
+    int32_t *task_status = nullptr;
+    uint64_t *task_nodes = nullptr;
+};
+// Cross-subtree maximality filter of split windows: window wi's tasks, in
+// subtree order, are task_of[win_task0[wi] .. win_task0[wi+1]).
+struct WFilterParams {
+    uint32_t d = 0;
+    uint32_t n_win = 0;
+    const uint32_t *win_task0 = nullptr;
+    const uint32_t *task_of = nullptr;
+    const uint64_t *task_off = nullptr;
+    const uint32_t *task_cnt = nullptr;
+    uint32_t *task_kept = nullptr;      // in: task_cnt; out: kept
+    const uint64_t *out_m = nullptr;
+    uint8_t *keep = nullptr;            // per arena slot (in: 1)
+    uint64_t *scratch = nullptr;        // per CTA scratch_words words
+    uint64_t scratch_words = 0;
+    int32_t *win_status = nullptr;      // per split window: 1 = scratch too small
+    uint32_t *next = nullptr;
+};
+struct WGatherParams {
+    uint64_t n_tasks = 0;
+    const uint64_t *task_off = nullptr;
+    const uint32_t *task_cnt = nullptr;
+    const uint64_t *task_dst = nullptr; // ~0 = skip
+    const uint8_t *keep = nullptr;      // null = keep all
+    const uint64_t *out_m = nullptr;
+    const uint32_t *out_s = nullptr;
+    uint64_t *dst_m = nullptr;
+    uint32_t *dst_s = nullptr;
 };
 size_t wmine_level_bytes(int mw);
-// blocks of 128 threads (4 warps)
-void launch_wmine(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
+size_t wmine_root_bytes(int mw);
+// blocks of 128 threads (4 warps; wfilter: 256 threads)
+void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
+void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
+void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st);
+void launch_wgather(const WGatherParams &p, int mw, unsigned blocks, cudaStream_t st);
 
 }  // namespace sg

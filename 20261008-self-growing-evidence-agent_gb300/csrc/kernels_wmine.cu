@@ -1,9 +1,9 @@
-// kernels_wmine.cu -- batched per-window MFI miner: one warp mines one window.
+// kernels_wmine.cu -- batched per-window MFI mining on the ring.
 //
 // The reference mines one window per engine process (code/pipeline/
 // skab_spike.py:61-80 builds the windows; the engines' DFS is
 // kernel_bitmap.cu:841-894); its result for a window is the MFI set of that
-// window's transactions at the window's floor, which this kernel reproduces.
+// window's transactions at the window's floor, which these kernels reproduce.
 //
 // Representation.  Items are the ring's dense ids 0..d-1 (d <= 64*MW); an
 // itemset is an MW-word mask.  A search node (H, T) holds its projected
@@ -12,11 +12,11 @@
 // nothing to any count below the node and are dropped).  The root's database
 // is the window itself, read from the ring's horizontal masks.
 //
-// Search.  Sequential depth-first over the set-enumeration tree, one node at
-// a time, children in ascending (support, id) order -- the order under which
-// a candidate found later is never a proper superset of one found earlier:
-// child j's subtree lacks item f_i of every earlier sibling i < j, which all
-// candidates of sibling i contain.  Every node applies
+// Search.  Depth-first over the set-enumeration tree, one node at a time per
+// warp, children in ascending (support, id) order -- the order under which a
+// candidate found later is never a proper superset of one found earlier in
+// the same subtree: child j's subtree lacks item f_i of every earlier sibling
+// i < j, which all candidates of sibling i contain.  Every node applies
 //   counts  c_e = |t(H u {e})|, e in T       (ballot popcounts over entries)
 //   PEP     c_e == sup(H) (and >= thr)       -> e joins H
 //   leaf    F = {e : thr <= c_e < sup(H)} empty: H is a candidate
@@ -25,13 +25,23 @@
 // and candidates are checked against the MFIs found so far that contain the
 // node's head (the "local MFI" list: the parent's list filtered to members
 // containing the child's head, plus everything found inside the parent's
-// subtree, which contains the parent's head by construction).  A candidate
-// that passes is maximal, so the window's pool is its exact MFI set.
+// subtree, which contains the parent's head by construction).
 //
-// Work is distributed by an atomic window counter (largest windows first);
-// every loop is bounded by list lengths, and any capacity overflow (list
-// stack, local-MFI stack, pool, depth) marks the window for the host-driven
-// wave miner instead of producing a partial result.
+// Work split.  A short window is one task: its warp searches the whole tree
+// and its pool is the exact MFI set.  A long window is split at the root:
+// wroot_kernel counts the root and sorts its frequent tail f_0..f_{k-1};
+// task (w, j) searches child j's subtree alone.  Tasks share no pool, so a
+// candidate of subtree j may sit inside a candidate of an earlier subtree
+// i < j (never of a later one, by the argument above); wfilter_kernel removes
+// exactly those with a vertical bitmap of the window's candidates.
+// wgather_kernel then writes the kept candidates in window order.
+//
+// Work is distributed by atomic counters (costliest tasks first); every
+// loop is bounded by list lengths, and any capacity overflow (entry stack,
+// local-MFI stack, pool, depth, filter scratch) marks the window for the
+// host-driven wave miner instead of producing a partial result.
+#include <cstddef>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -45,12 +55,15 @@ template <int MW> struct Mask {
     uint64_t w[MW];
 };
 
-template <int MW> __device__ __forceinline__ bool m_has(const Mask<MW> &m, uint32_t e) {
-    uint64_t x = 0;
+template <int MW> __device__ __forceinline__ uint64_t m_word(const Mask<MW> &m, uint32_t i) {
+    uint64_t r = 0;
 #pragma unroll
     for (int k = 0; k < MW; ++k)
-        if ((uint32_t)k == (e >> 6)) x = m.w[k];
-    return (x >> (e & 63)) & 1ull;
+        if ((uint32_t)k == i) r = m.w[k];
+    return r;
+}
+template <int MW> __device__ __forceinline__ bool m_has(const Mask<MW> &m, uint32_t e) {
+    return (m_word(m, e >> 6) >> (e & 63)) & 1ull;
 }
 template <int MW> __device__ __forceinline__ void m_set(Mask<MW> &m, uint32_t e) {
 #pragma unroll
@@ -98,14 +111,6 @@ template <int MW> __device__ __forceinline__ void m_store(uint64_t *p, const Mas
 #pragma unroll
     for (int i = 0; i < MW; i += 2) *reinterpret_cast<ulonglong2 *>(p + i) = make_ulonglong2(m.w[i], m.w[i + 1]);
 }
-// word i of m without a dynamically indexed register array
-template <int MW> __device__ __forceinline__ uint64_t m_word(const Mask<MW> &m, uint32_t i) {
-    uint64_t r = 0;
-#pragma unroll
-    for (int k = 0; k < MW; ++k)
-        if ((uint32_t)k == i) r = m.w[k];
-    return r;
-}
 template <int MW> __device__ __forceinline__ Mask<MW> warp_or(const Mask<MW> &m) {
     Mask<MW> r;
 #pragma unroll
@@ -119,24 +124,242 @@ template <int MW> __device__ __forceinline__ Mask<MW> warp_or(const Mask<MW> &m)
 
 // Per-level record of the search stack (global memory, one stack per warp).
 template <int MW> struct alignas(16) WLevel {
-    uint64_t hp[MW];      // head after PEP
-    uint64_t list_off;    // first entry of this node's projected database (levels >= 1)
+    uint64_t hp[MW];        // head after PEP
+    uint64_t list_off;      // first entry of this node's projected database
     uint32_t list_n;
     uint32_t lm_off, lm_n;  // local-MFI list (pool indices)
-    uint32_t entry;       // pool size when the node was entered
-    uint32_t k, j;        // frequent tail size, next child
-    uint8_t f[128];       // frequent tail, ascending (support, id)
-    uint32_t c[128];      // supports of f
+    uint32_t entry;         // pool size when the node was entered
+    uint32_t k, j;          // frequent tail size, next child
+    uint8_t f[128];         // frequent tail, ascending (support, id)
+    uint32_t c[128];        // supports of f
 };
+
+// Root of a split window (wroot_kernel -> wtask_kernel).
+template <int MW> struct alignas(16) WRoot {
+    uint64_t hp[MW];        // root head after PEP (items in every transaction)
+    uint64_t cand[MW];      // the window's only MFI when the root is terminal
+    uint32_t cand_sup;
+    uint32_t has_cand;      // 1: the MFI set is {cand}; 0: the tasks (k of them) hold it
+    uint32_t k;
+    uint32_t n;             // window length
+    uint8_t f[128];
+    uint32_t c[128];
+};
+
+// the host reads these fields of the root records (ring.cu)
+static_assert(offsetof(WRoot<2>, cand) == 16 && offsetof(WRoot<2>, cand_sup) == 32 &&
+                  offsetof(WRoot<2>, has_cand) == 36 && offsetof(WRoot<2>, k) == 40 && offsetof(WRoot<2>, f) == 48 &&
+                  offsetof(WRoot<2>, c) == 176,
+              "root record layout read by sgfim_ring_mine_windows");
 
 // The search stack holds itemsets of up to kWDepth - 1 items.
 constexpr int kWDepth = 48;
 // chunks of 32 entries loaded before any is processed (memory-level parallelism)
 constexpr int kU = 4;
 
+// One projected-database entry: ring slot (start + i) of the window, or entry
+// i of the warp's stack.
+template <int MW> __device__ __forceinline__ const uint64_t *entry_ptr(bool ring, const WMineParams &p, uint64_t start,
+                                                                      const uint64_t *lists, uint64_t off, uint32_t i) {
+    return ring ? p.hm + ((start + i) & p.cap_mask) * MW : lists + (off + i) * MW;
+}
+
+// c_e over the database (lane 0 accumulates into the warp's counters cnt[128]).
+template <int MW>
+__device__ __forceinline__ void count_items(bool ring, const WMineParams &p, uint64_t start, const uint64_t *lists,
+                                            uint64_t off, uint32_t n, const Mask<MW> &T, uint32_t *cnt,
+                                            uint32_t lane) {
+    for (uint32_t q = lane; q < 128; q += 32) cnt[q] = 0;
+    __syncwarp();
+    for (uint32_t b = 0; b < n; b += 32 * kU) {
+        Mask<MW> m[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = b + u * 32 + lane;
+            m[u] = i < n ? m_and(m_load<MW>(entry_ptr<MW>(ring, p, start, lists, off, i)), T) : m_zero<MW>();
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const Mask<MW> om = warp_or(m[u]);
+#pragma unroll
+            for (int ww = 0; ww < MW; ++ww) {
+                const uint64_t mine = m[u].w[ww];
+                uint64_t x = om.w[ww];
+                while (x) {
+                    const uint32_t bit = __ffsll((long long)x) - 1;
+                    x &= x - 1;
+                    const uint32_t c = __popc(__ballot_sync(kFull, (mine >> bit) & 1ull));
+                    if (lane == 0) cnt[ww * 64 + bit] += c;
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// PEP items P and frequent tail F of a node from its counts.
+template <int MW>
+__device__ __forceinline__ void classify(const Mask<MW> &T, const uint32_t *cnt, uint32_t d, uint32_t thr, uint32_t sup,
+                                         uint32_t lane, Mask<MW> &P, Mask<MW> &F) {
+    P = m_zero<MW>();
+    F = m_zero<MW>();
+#pragma unroll
+    for (int q = 0; q < 2 * MW; ++q) {
+        const uint32_t e = q * 32 + lane;
+        const bool inT = e < d && ((T.w[q >> 1] >> ((q & 1) * 32 + lane)) & 1ull);
+        const uint32_t c = inT ? cnt[e] : 0;
+        const uint32_t bp = __ballot_sync(kFull, inT && c >= thr && c == sup);
+        const uint32_t bf = __ballot_sync(kFull, inT && c >= thr && c < sup);
+        P.w[q >> 1] |= (uint64_t)bp << ((q & 1) * 32);
+        F.w[q >> 1] |= (uint64_t)bf << ((q & 1) * 32);
+    }
+}
+
+// |{entries containing F}|
+template <int MW>
+__device__ __forceinline__ uint32_t count_superset(bool ring, const WMineParams &p, uint64_t start,
+                                                   const uint64_t *lists, uint64_t off, uint32_t n,
+                                                   const Mask<MW> &F, uint32_t lane) {
+    uint32_t cf = 0;
+    for (uint32_t b = 0; b < n; b += 32 * kU) {
+        bool h[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = b + u * 32 + lane;
+            h[u] = i < n && m_sub(F, m_load<MW>(entry_ptr<MW>(ring, p, start, lists, off, i)));
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) cf += __popc(__ballot_sync(kFull, h[u]));
+    }
+    return cf;
+}
+
+// F sorted by (count, id) ascending into f[], c[] (the lanes own the 4*MW/2
+// items lane, lane+32, ...; one pass over F compares against all of them).
+template <int MW>
+__device__ __forceinline__ void sort_tail(const Mask<MW> &F, const uint32_t *cnt, uint32_t lane, uint8_t *f,
+                                          uint32_t *c) {
+    uint32_t ce[2 * MW], rank[2 * MW];
+#pragma unroll
+    for (int q = 0; q < 2 * MW; ++q) {
+        const uint32_t e = q * 32 + lane;
+        ce[q] = ((F.w[q >> 1] >> ((q & 1) * 32 + lane)) & 1ull) ? cnt[e] : 0xffffffffu;
+        rank[q] = 0;
+    }
+#pragma unroll
+    for (int ww = 0; ww < MW; ++ww) {
+        uint64_t x = F.w[ww];
+        while (x) {
+            const uint32_t e2 = ww * 64 + (__ffsll((long long)x) - 1);
+            x &= x - 1;
+            const uint32_t c2 = cnt[e2];
+#pragma unroll
+            for (int q = 0; q < 2 * MW; ++q) {
+                const uint32_t e = q * 32 + lane;
+                rank[q] += (c2 < ce[q]) || (c2 == ce[q] && e2 < e);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 2 * MW; ++q) {
+        if (ce[q] != 0xffffffffu) {
+            f[rank[q]] = (uint8_t)(q * 32 + lane);
+            c[rank[q]] = ce[q];
+        }
+    }
+}
+
+// Child database: entries holding e, restricted to Tc, non-empty, written at
+// dst .. dst+cn of the warp's stack.  Returns cn, or 0xffffffff on overflow.
+template <int MW>
+__device__ __forceinline__ uint32_t build_child(bool ring, const WMineParams &p, uint64_t start, uint64_t *lists,
+                                                uint64_t src_off, uint32_t src_n, uint32_t e, const Mask<MW> &Tc,
+                                                uint64_t dst, uint32_t lane) {
+    uint32_t cn = 0;
+    for (uint32_t b = 0; b < src_n; b += 32 * kU) {
+        Mask<MW> m[kU];
+        bool keep[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = b + u * 32 + lane;
+            m[u] = m_zero<MW>();
+            keep[u] = false;
+            if (i < src_n) {
+                const Mask<MW> r = m_load<MW>(entry_ptr<MW>(ring, p, start, lists, src_off, i));
+                m[u] = m_and(r, Tc);
+                keep[u] = m_has(r, e) && m_nz(m[u]);
+            }
+        }
+        // the child's entries go after the source's: writes never touch entries still to be read
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t bal = __ballot_sync(kFull, keep[u]);
+            const uint64_t pos = dst + cn + __popc(bal & ((1u << lane) - 1));
+            if (keep[u] && pos < p.list_cap) m_store(lists + pos * MW, m[u]);
+            cn += __popc(bal);
+        }
+    }
+    return dst + cn > p.list_cap ? 0xffffffffu : cn;
+}
+
 }  // namespace
 
-template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParams p) {
+// ------------------------------------------------------------------ roots
+template <int MW> __global__ void __launch_bounds__(128) wroot_kernel(WMineParams p) {
+    __shared__ uint32_t s_cnt[4][128];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    uint32_t *cnt = s_cnt[wib];
+    WRoot<MW> *roots = reinterpret_cast<WRoot<MW> *>(p.roots);
+    for (;;) {
+        uint32_t wi = 0;
+        if (lane == 0) wi = atomicAdd(p.next + 1, 1u);
+        wi = __shfl_sync(kFull, wi, 0);
+        if (wi >= p.n_split) break;
+        const uint32_t w = p.split_win[wi];
+        const uint64_t start = p.starts[w];
+        const uint32_t n = p.lens[w];
+        const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
+        Mask<MW> T = m_zero<MW>();
+        for (uint32_t e = 0; e < p.d; ++e) m_set(T, e);
+        count_items<MW>(true, p, start, nullptr, 0, n, T, cnt, lane);
+        Mask<MW> P, F;
+        classify<MW>(T, cnt, p.d, thr, n, lane, P, F);
+        uint32_t k = 0;
+#pragma unroll
+        for (int i = 0; i < MW; ++i) k += __popcll(F.w[i]);
+        WRoot<MW> &R = roots[w];
+        uint32_t has = 0, csup = 0;
+        Mask<MW> cand = P;   // root head after PEP (H = {} at the root)
+        if (k == 0) {
+            has = m_nz(P) ? 1u : 0u;
+            csup = n;
+        } else {
+            const uint32_t cf = count_superset<MW>(true, p, start, nullptr, 0, n, F, lane);
+            if (cf >= thr) {
+                has = 1;
+                csup = cf;
+#pragma unroll
+                for (int i = 0; i < MW; ++i) cand.w[i] |= F.w[i];
+            }
+        }
+        if (!has && k) sort_tail<MW>(F, cnt, lane, R.f, R.c);
+        if (lane < MW) {
+            R.hp[lane] = m_word(P, lane);
+            R.cand[lane] = m_word(cand, lane);
+        }
+        if (lane == 0) {
+            R.cand_sup = csup;
+            R.has_cand = has;
+            R.k = has ? 0 : k;
+            R.n = n;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ tasks
+template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParams p) {
     __shared__ uint32_t s_cnt[4][128];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
@@ -147,14 +370,17 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
     uint64_t *pool = p.pool_m + warp * (uint64_t)p.pool_cap * MW;
     uint32_t *pool_s = p.pool_s + warp * (uint64_t)p.pool_cap;
     WLevel<MW> *LV = reinterpret_cast<WLevel<MW> *>(p.levels) + warp * kWDepth;
+    const WRoot<MW> *roots = reinterpret_cast<const WRoot<MW> *>(p.roots);
     const uint32_t d = p.d;
 
     for (;;) {
-        uint32_t wi = 0;
-        if (lane == 0) wi = atomicAdd(p.next, 1u);
-        wi = __shfl_sync(kFull, wi, 0);
-        if (wi >= p.n_win) break;
-        const uint32_t w = p.order[wi];
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(p.next, 1u);
+        ti = __shfl_sync(kFull, ti, 0);
+        if (ti >= p.n_tasks) break;
+        const uint32_t t = p.task_order[ti];
+        const uint32_t w = p.task_win[t];
+        const uint32_t child = p.task_child[t];
         const uint64_t start = p.starts[w];
         const uint32_t n = p.lens[w];
         const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
@@ -162,13 +388,29 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
         uint32_t np = 0;
         uint64_t nodes = 0;
 
-        // current node
-        int l = 0;
+        // the task's first node: the whole window, or child `child` of its root
+        bool ring0 = child == kWholeWindow;
         Mask<MW> H = m_zero<MW>(), T = m_zero<MW>();
-        for (uint32_t e = 0; e < d; ++e) m_set(T, e);
-        uint32_t sup = n;
+        uint32_t sup = n, list_n = n;
+        if (ring0) {
+            for (uint32_t e = 0; e < d; ++e) m_set(T, e);
+        } else {
+            const WRoot<MW> &R = roots[w];
+            const uint32_t k = R.k;
+            for (uint32_t q = child + 1 + lane; q < k; q += 32) m_set(T, R.f[q]);
+            T = warp_or(T);
+            H = m_load<MW>(R.hp);
+            const uint32_t e = R.f[child];
+            m_set(H, e);
+            sup = R.c[child];
+            list_n = 0;
+            if (m_nz(T)) {
+                list_n = build_child<MW>(true, p, start, lists, 0, n, e, T, 0, lane);
+                if (list_n == 0xffffffffu) status = 1;
+            }
+        }
+        int l = 0;
         uint64_t list_off = 0;
-        uint32_t list_n = n;       // root: the window in the ring
         uint32_t lm_off = 0, lm_n = 0, entry = 0;
         bool expand = true;
 
@@ -176,50 +418,10 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
             if (expand) {
                 expand = false;
                 ++nodes;
-                const bool root = l == 0;
-                // ---- counts over the projected database
-                for (uint32_t q = lane; q < 128; q += 32) cnt[q] = 0;
-                __syncwarp();
-                for (uint32_t b = 0; b < list_n; b += 32 * kU) {
-                    Mask<MW> m[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) {
-                        const uint32_t i = b + u * 32 + lane;
-                        m[u] = m_zero<MW>();
-                        if (i < list_n) {
-                            const uint64_t *src =
-                                root ? p.hm + ((start + i) & p.cap_mask) * MW : lists + (list_off + i) * MW;
-                            m[u] = m_and(m_load<MW>(src), T);
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) {
-                        const Mask<MW> om = warp_or(m[u]);
-#pragma unroll
-                        for (int ww = 0; ww < MW; ++ww) {
-                            uint64_t x = om.w[ww];
-                            while (x) {
-                                const uint32_t bit = __ffsll((long long)x) - 1;
-                                x &= x - 1;
-                                const uint32_t c = __popc(__ballot_sync(kFull, (m[u].w[ww] >> bit) & 1ull));
-                                if (lane == 0) cnt[ww * 64 + bit] += c;
-                            }
-                        }
-                    }
-                }
-                __syncwarp();
-                // ---- PEP and the frequent tail
-                Mask<MW> P = m_zero<MW>(), F = m_zero<MW>();
-#pragma unroll
-                for (int q = 0; q < 2 * MW; ++q) {
-                    const uint32_t e = q * 32 + lane;
-                    const bool inT = e < d && ((T.w[q >> 1] >> ((q & 1) * 32 + lane)) & 1ull);
-                    const uint32_t c = inT ? cnt[e] : 0;
-                    const uint32_t bp = __ballot_sync(kFull, inT && c >= thr && c == sup);
-                    const uint32_t bf = __ballot_sync(kFull, inT && c >= thr && c < sup);
-                    P.w[q >> 1] |= (uint64_t)bp << ((q & 1) * 32);
-                    F.w[q >> 1] |= (uint64_t)bf << ((q & 1) * 32);
-                }
+                const bool ring = ring0 && l == 0;
+                count_items<MW>(ring, p, start, lists, list_off, list_n, T, cnt, lane);
+                Mask<MW> P, F;
+                classify<MW>(T, cnt, d, thr, sup, lane, P, F);
                 Mask<MW> Hp, Q;
                 uint32_t k = 0;
 #pragma unroll
@@ -256,22 +458,7 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
                     continue;
                 }
                 // ---- FHUT: support of H u P u F
-                uint32_t cf = 0;
-                for (uint32_t b = 0; b < list_n; b += 32 * kU) {
-                    bool h[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) {
-                        const uint32_t i = b + u * 32 + lane;
-                        h[u] = false;
-                        if (i < list_n) {
-                            const uint64_t *src =
-                                root ? p.hm + ((start + i) & p.cap_mask) * MW : lists + (list_off + i) * MW;
-                            h[u] = m_sub(F, m_load<MW>(src));
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) cf += __popc(__ballot_sync(kFull, h[u]));
-                }
+                const uint32_t cf = count_superset<MW>(ring, p, start, lists, list_off, list_n, F, lane);
                 if (cf >= thr) {
                     if (np >= p.pool_cap) { status = 1; break; }
                     if (lane < MW) pool[(uint64_t)np * MW + lane] = m_word(Q, lane);
@@ -284,27 +471,7 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
                 }
                 // ---- record the node: frequent tail sorted by (support, id)
                 WLevel<MW> &A = LV[l];
-#pragma unroll
-                for (int q = 0; q < 2 * MW; ++q) {
-                    const uint32_t e = q * 32 + lane;
-                    const bool isF = (F.w[q >> 1] >> ((q & 1) * 32 + lane)) & 1ull;
-                    const uint32_t ce = isF ? cnt[e] : 0;
-                    uint32_t rank = 0;
-#pragma unroll
-                    for (int ww = 0; ww < MW; ++ww) {
-                        uint64_t x = F.w[ww];
-                        while (x) {
-                            const uint32_t e2 = ww * 64 + (__ffsll((long long)x) - 1);
-                            x &= x - 1;
-                            const uint32_t c2 = cnt[e2];
-                            rank += (c2 < ce) || (c2 == ce && e2 < e);
-                        }
-                    }
-                    if (isF) {
-                        A.f[rank] = (uint8_t)e;
-                        A.c[rank] = ce;
-                    }
-                }
+                sort_tail<MW>(F, cnt, lane, A.f, A.c);
                 if (lane < MW) A.hp[lane] = m_word(Hp, lane);
                 if (lane == 0) {
                     A.list_off = list_off;
@@ -330,45 +497,18 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
             const uint32_t e = A.f[j];
             const uint32_t csup = A.c[j];
             Mask<MW> Tc = m_zero<MW>();
-            for (uint32_t q = j + 1 + lane; q < k; q += 32) {
-                m_set(Tc, A.f[q]);
-            }
+            for (uint32_t q = j + 1 + lane; q < k; q += 32) m_set(Tc, A.f[q]);
             Tc = warp_or(Tc);
             Mask<MW> Hc = m_load<MW>(A.hp);
             m_set(Hc, e);
-            const bool proot = l == 0;
+            const bool pring = ring0 && l == 0;
             const uint64_t p_off = A.list_off;
             const uint32_t p_n = A.list_n;
-            // child database: entries with e, restricted to the child's tail, non-empty
-            const uint64_t c_off = proot ? 0 : p_off + p_n;
+            const uint64_t c_off = pring ? 0 : p_off + p_n;
             uint32_t cn = 0;
             if (m_nz(Tc)) {
-                for (uint32_t b = 0; b < p_n; b += 32 * kU) {
-                    Mask<MW> m[kU];
-                    bool keep[kU];
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) {
-                        const uint32_t i = b + u * 32 + lane;
-                        m[u] = m_zero<MW>();
-                        keep[u] = false;
-                        if (i < p_n) {
-                            const uint64_t *src =
-                                proot ? p.hm + ((start + i) & p.cap_mask) * MW : lists + (p_off + i) * MW;
-                            const Mask<MW> r = m_load<MW>(src);
-                            m[u] = m_and(r, Tc);
-                            keep[u] = m_has(r, e) && m_nz(m[u]);
-                        }
-                    }
-                    // the child's entries go after the parent's: writes never touch entries still to be read
-#pragma unroll
-                    for (int u = 0; u < kU; ++u) {
-                        const uint32_t bal = __ballot_sync(kFull, keep[u]);
-                        const uint64_t pos = c_off + cn + __popc(bal & ((1u << lane) - 1));
-                        if (keep[u] && pos < p.list_cap) m_store(lists + pos * MW, m[u]);
-                        cn += __popc(bal);
-                    }
-                }
-                if (c_off + cn > p.list_cap) { status = 1; break; }
+                cn = build_child<MW>(pring, p, start, lists, p_off, p_n, e, Tc, c_off, lane);
+                if (cn == 0xffffffffu) { status = 1; break; }
             }
             // child local-MFI list: members containing the child's head
             const uint32_t c_lm = A.lm_off + A.lm_n;
@@ -412,7 +552,7 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
             expand = true;
         }
 
-        // ---- publish the window's MFIs
+        // ---- publish the task's candidates
         uint64_t off = 0;
         if (status == 0) {
             if (lane == 0) off = atomicAdd(p.out_pos, (unsigned long long)np);
@@ -426,22 +566,145 @@ template <int MW> __global__ void __launch_bounds__(128) wmine_kernel(WMineParam
             }
         }
         if (lane == 0) {
-            p.win_off[w] = off;
-            p.win_cnt[w] = status == 0 ? np : 0;
-            p.win_status[w] = status;
-            p.win_nodes[w] = nodes;
+            p.task_off[t] = off;
+            p.task_cnt[t] = status == 0 ? np : 0;
+            p.task_status[t] = status;
+            p.task_nodes[t] = nodes;
         }
         __syncwarp();
     }
 }
 
-size_t wmine_level_bytes(int mw) {
-    return mw == 2 ? sizeof(WLevel<2>) * kWDepth : 0;
+// ------------------------------------------------------------------ cross-task filter
+// One CTA per split window: the window's candidates in task order (subtree
+// j ascending) get a vertical bitmap rows[e][p]; candidate p of subtree j is
+// dropped when the AND of its items' rows has a bit below the first
+// candidate of subtree j.  keep[] is written per arena slot, kept[] per task.
+template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterParams p) {
+    __shared__ uint64_t s_first[129];    // first candidate (window order) of each task, + total
+    __shared__ uint32_t s_w;
+    uint64_t *rows = p.scratch + (uint64_t)blockIdx.x * p.scratch_words;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_w = atomicAdd(p.next, 1u);
+        __syncthreads();
+        const uint32_t wi = s_w;
+        if (wi >= p.n_win) break;
+        const uint32_t t0 = p.win_task0[wi], nt = p.win_task0[wi + 1] - t0;   // tasks of this window, j order
+        if (threadIdx.x == 0) {
+            uint64_t acc = 0;
+            for (uint32_t j = 0; j < nt; ++j) {
+                s_first[j] = acc;
+                acc += p.task_cnt[p.task_of[t0 + j]];
+            }
+            s_first[nt] = acc;
+        }
+        __syncthreads();
+        const uint64_t M = s_first[nt];
+        const uint64_t W = (M + 63) / 64;
+        if (W * p.d > p.scratch_words) {
+            if (threadIdx.x == 0) p.win_status[wi] = 1;
+            continue;
+        }
+        for (uint64_t i = threadIdx.x; i < W * p.d; i += blockDim.x) rows[i] = 0;
+        __syncthreads();
+        // candidate q (window order) -> task j, arena slot
+        for (uint64_t q = threadIdx.x; q < M; q += blockDim.x) {
+            uint32_t j = 0;
+            while (s_first[j + 1] <= q) ++j;
+            const uint64_t slot = p.task_off[p.task_of[t0 + j]] + (q - s_first[j]);
+            const Mask<MW> m = m_load<MW>(p.out_m + slot * MW);
+#pragma unroll
+            for (int ww = 0; ww < MW; ++ww) {
+                uint64_t x = m.w[ww];
+                while (x) {
+                    const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+                    x &= x - 1;
+                    atomicOr(reinterpret_cast<unsigned long long *>(rows + (uint64_t)e * W + (q >> 6)),
+                             1ull << (q & 63));
+                }
+            }
+        }
+        __syncthreads();
+        for (uint64_t q = threadIdx.x; q < M; q += blockDim.x) {
+            uint32_t j = 0;
+            while (s_first[j + 1] <= q) ++j;
+            const uint32_t t = p.task_of[t0 + j];
+            const uint64_t slot = p.task_off[t] + (q - s_first[j]);
+            bool keep = true;
+            const uint64_t lim = s_first[j];   // candidates of earlier subtrees: [0, lim)
+            if (lim) {
+                const Mask<MW> m = m_load<MW>(p.out_m + slot * MW);
+                uint32_t e0 = 0;
+                for (int ww = 0; ww < MW; ++ww)
+                    if (m.w[ww]) { e0 = ww * 64 + (__ffsll((long long)m.w[ww]) - 1); break; }
+                for (uint64_t wd = 0; wd * 64 < lim && keep; ++wd) {
+                    uint64_t v = rows[(uint64_t)e0 * W + wd];
+                    if (wd * 64 + 64 > lim) v &= (1ull << (lim - wd * 64)) - 1;
+#pragma unroll
+                    for (int ww = 0; ww < MW; ++ww) {
+                        uint64_t x = m.w[ww];
+                        while (x && v) {
+                            const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+                            x &= x - 1;
+                            v &= rows[(uint64_t)e * W + wd];
+                        }
+                    }
+                    keep = v == 0;
+                }
+            }
+            p.keep[slot] = keep ? 1 : 0;
+            if (!keep) atomicSub(&p.task_kept[t], 1u);
+        }
+    }
 }
 
-void launch_wmine(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
-    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "wmine supports 2 mask words", __FILE__, __LINE__);
-    wmine_kernel<2><<<blocks, 128, 0, st>>>(p);
+// ------------------------------------------------------------------ gather
+// One warp per task: its kept candidates, in emission order, to dst.
+template <int MW> __global__ void __launch_bounds__(128) wgather_kernel(WGatherParams p) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = warp; t < p.n_tasks; t += n_warps) {
+        const uint64_t src = p.task_off[t];
+        const uint32_t n = p.task_cnt[t];
+        uint64_t dst = p.task_dst[t];
+        if (dst == ~0ull) continue;
+        for (uint32_t b = 0; b < n; b += 32) {
+            const uint32_t i = b + lane;
+            const bool keep = i < n && (!p.keep || p.keep[src + i]);
+            const uint32_t bal = __ballot_sync(kFull, keep);
+            if (keep) {
+                const uint64_t pos = dst + __popc(bal & ((1u << lane) - 1));
+                m_store<MW>(p.dst_m + pos * MW, m_load<MW>(p.out_m + (src + i) * MW));
+                p.dst_s[pos] = p.out_s[src + i];
+            }
+            dst += __popc(bal);
+        }
+    }
+}
+
+size_t wmine_level_bytes(int mw) { return mw == 2 ? sizeof(WLevel<2>) * kWDepth : 0; }
+size_t wmine_root_bytes(int mw) { return mw == 2 ? sizeof(WRoot<2>) : 0; }
+
+void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
+    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
+    wroot_kernel<2><<<blocks, 128, 0, st>>>(p);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
+    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
+    wtask_kernel<2><<<blocks, 128, 0, st>>>(p);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st) {
+    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
+    wfilter_kernel<2><<<blocks, 256, 0, st>>>(p);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+void launch_wgather(const WGatherParams &p, int mw, unsigned blocks, cudaStream_t st) {
+    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
+    wgather_kernel<2><<<blocks, 128, 0, st>>>(p);
     SG_CUDA_TRY(cudaGetLastError());
 }
 

@@ -327,60 +327,75 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
         }
     } release{r, starts, n_windows, ev};
 
-    // per-window results: [first, count) in `found` (batched) or in `wave_sets`
-    std::vector<uint64_t> res_off(n_windows, 0), res_cnt(n_windows, 0), nodes(n_windows, 0);
+    // per-window results
+    std::vector<uint64_t> res_cnt(n_windows, 0), nodes(n_windows, 0);
     std::vector<int32_t> status(n_windows, SGFIM_OK);
     std::vector<uint8_t> batched(n_windows, 0);
-    std::vector<uint64_t> found_m;
-    std::vector<uint32_t> found_s;
-    std::vector<uint64_t> wave;   // windows for the wave miner
+    std::vector<uint64_t> root_cand;         // (window, mask words...) of split windows with a terminal root
+    std::vector<uint32_t> root_cand_sup;
+    std::vector<uint64_t> wave;              // windows for the wave miner
     double kernel_ms = 0.0;
     uint32_t launches = 0;
+    // batched results, gathered on the device into window order at the end
+    std::vector<uint64_t> task_dst;          // per task: destination slot (~0 = dropped)
+    uint64_t n_tasks_total = 0;
+    WindowWorkspace &ws = h->wws;
+    uint64_t *d_task_off = nullptr;
+    uint32_t *d_task_cnt = nullptr;
+    uint8_t *d_keep = nullptr;
+    std::vector<uint64_t> t_win_of;          // task -> window
+    std::vector<uint32_t> kept;              // per task: candidates kept
     try {
         SG_CUDA_TRY(cudaSetDevice(h->device));
         cudaStream_t st = h->stream;
         if (r->hm.ptr && n_windows) {
-            WindowWorkspace &ws = h->wws;
+            // windows of at least kSplitMin transactions are split at the root
+            constexpr uint64_t kSplitMin = 4096;
             uint64_t max_len = 0;
-            for (uint64_t w = 0; w < n_windows; ++w) max_len = std::max(max_len, lens[w]);
+            std::vector<uint32_t> split;
+            for (uint64_t w = 0; w < n_windows; ++w) {
+                max_len = std::max(max_len, lens[w]);
+                if (lens[w] >= kSplitMin) split.push_back((uint32_t)w);
+            }
             const uint64_t list_cap = std::min<uint64_t>(std::max<uint64_t>(8192, 2 * max_len + 1024), 1ull << 30);
             const uint64_t lmfi_cap = 1u << 16, pool_cap = 1u << 16;
             const size_t per_warp = list_cap * mw * 8 + lmfi_cap * 4 + pool_cap * (mw * 8 + 4) + wmine_level_bytes(mw);
-            uint64_t warps = std::min<uint64_t>((uint64_t)h->n_sm * 16, (n_windows + 3) & ~3ull);
+            uint64_t warps = (uint64_t)h->n_sm * 24;
             warps = std::min<uint64_t>(warps, std::max<uint64_t>(4, (h->hbm_budget / 2) / per_warp));
             warps = std::max<uint64_t>(4, warps & ~3ull);
-            const uint64_t out_cap =
-                std::max<uint64_t>(1u << 20, std::min<uint64_t>(n_windows * 32768, (h->hbm_budget / 4) / (mw * 8 + 4)));
+            const size_t cand_bytes = mw * 8 + 4 + 1;
+            const uint64_t out_cap = std::max<uint64_t>(
+                1u << 20, std::min<uint64_t>(n_windows * 65536, (h->hbm_budget / 4) / cand_bytes));
+            const size_t root_b = wmine_root_bytes(mw);
             ws.lists.reserve(warps * list_cap * mw * 8, st);
             ws.lmfi.reserve(warps * lmfi_cap * 4, st);
             ws.pool_m.reserve(warps * pool_cap * mw * 8, st);
             ws.pool_s.reserve(warps * pool_cap * 4, st);
             ws.levels.reserve(warps * wmine_level_bytes(mw), st);
             ws.out_m.reserve(out_cap * mw * 8, st);
-            ws.out_s.reserve(out_cap * 4, st);
+            ws.out_s.reserve(out_cap * 5, st);   // supports, then the keep flags
             ws.ctrl.reserve(256, st);
-            // window table: starts u64 | lens u32 | thrs u32 | order u32
+            // window table: starts u64 | lens u32 | thrs u32 | split u32
             const size_t tb = n_windows * 8 + 3 * n_windows * 4;
             ws.table.reserve(tb, st);
             ws.h_table.reserve(tb);
-            // results: off u64 | nodes u64 | cnt u32 | status i32
-            const size_t rb = n_windows * 24;
-            ws.res.reserve(rb, st);
-            ws.h_res.reserve(rb);
             uint64_t *t_start = ws.h_table.as<uint64_t>();
             uint32_t *t_len = reinterpret_cast<uint32_t *>(t_start + n_windows);
             uint32_t *t_thr = t_len + n_windows;
-            uint32_t *t_order = t_thr + n_windows;
+            uint32_t *t_split = t_thr + n_windows;
             for (uint64_t w = 0; w < n_windows; ++w) {
                 t_start[w] = starts[w];
                 t_len[w] = (uint32_t)lens[w];
                 t_thr[w] = min_counts[w] ? min_counts[w] : 1;
             }
-            std::vector<uint32_t> pending(n_windows);
-            for (uint64_t w = 0; w < n_windows; ++w) pending[w] = (uint32_t)w;
-            // largest windows first
-            std::stable_sort(pending.begin(), pending.end(), [&](uint32_t a, uint32_t b) { return lens[a] > lens[b]; });
+            if (!split.empty()) memcpy(t_split, split.data(), split.size() * 4);
             SG_CUDA_TRY(cudaStreamWaitEvent(st, ev, 0));
+            SG_CUDA_TRY(cudaMemcpyAsync(ws.table.ptr, ws.h_table.ptr, tb, cudaMemcpyHostToDevice, st));
+            SG_CUDA_TRY(cudaMemsetAsync(ws.ctrl.ptr, 0, 256, st));
+            uint64_t *d_start = ws.table.as<uint64_t>();
+            uint32_t *d_len = reinterpret_cast<uint32_t *>(d_start + n_windows);
+            uint32_t *d_thr = d_len + n_windows;
+            uint32_t *d_split = d_thr + n_windows;
             cudaEvent_t k0, k1;
             SG_CUDA_TRY(cudaEventCreate(&k0));
             SG_CUDA_TRY(cudaEventCreate(&k1));
@@ -388,95 +403,238 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 cudaEvent_t a, b;
                 ~EvPair() { cudaEventDestroy(a); cudaEventDestroy(b); }
             } evp{k0, k1};
-            uint64_t *d_start = ws.table.as<uint64_t>();
-            uint32_t *d_len = reinterpret_cast<uint32_t *>(d_start + n_windows);
-            uint32_t *d_thr = d_len + n_windows;
-            uint32_t *d_order = d_thr + n_windows;
-            uint64_t *d_off = ws.res.as<uint64_t>();
-            uint64_t *d_nodes = d_off + n_windows;
-            uint32_t *d_cnt = reinterpret_cast<uint32_t *>(d_nodes + n_windows);
-            int32_t *d_status = reinterpret_cast<int32_t *>(d_cnt + n_windows);
-            bool first = true;
-            while (!pending.empty()) {
-                memcpy(t_order, pending.data(), pending.size() * 4);
-                SG_CUDA_TRY(cudaMemcpyAsync(ws.table.ptr, ws.h_table.ptr, first ? tb : 0, cudaMemcpyHostToDevice, st));
-                SG_CUDA_TRY(cudaMemcpyAsync(d_order, t_order, pending.size() * 4, cudaMemcpyHostToDevice, st));
-                first = false;
-                SG_CUDA_TRY(cudaMemsetAsync(ws.ctrl.ptr, 0, 256, st));
-                WMineParams p;
-                p.hm = r->hm.as<uint64_t>();
-                p.cap_mask = cap_bits - 1;
-                p.d = r->d;
-                p.starts = d_start;
-                p.lens = d_len;
-                p.thrs = d_thr;
-                p.order = d_order;
-                p.n_win = (uint32_t)pending.size();
-                p.next = ws.ctrl.as<uint32_t>();
-                p.out_pos = reinterpret_cast<unsigned long long *>(ws.ctrl.as<uint64_t>() + 1);
-                p.lists = ws.lists.as<uint64_t>();
-                p.list_cap = (uint32_t)list_cap;
-                p.lmfi = ws.lmfi.as<uint32_t>();
-                p.lmfi_cap = (uint32_t)lmfi_cap;
-                p.pool_m = ws.pool_m.as<uint64_t>();
-                p.pool_s = ws.pool_s.as<uint32_t>();
-                p.pool_cap = (uint32_t)pool_cap;
-                p.levels = ws.levels.ptr;
-                p.out_m = ws.out_m.as<uint64_t>();
-                p.out_s = ws.out_s.as<uint32_t>();
-                p.out_cap = out_cap;
-                p.win_off = d_off;
-                p.win_cnt = d_cnt;
-                p.win_status = d_status;
-                p.win_nodes = d_nodes;
-                const uint64_t use_warps = std::min<uint64_t>(warps, (pending.size() + 3) & ~3ull);
+            auto timed_ms = [&]() {
+                float ms = 0.f;
+                SG_CUDA_TRY(cudaEventElapsedTime(&ms, k0, k1));
+                return (double)ms;
+            };
+            WMineParams p;
+            p.hm = r->hm.as<uint64_t>();
+            p.cap_mask = cap_bits - 1;
+            p.d = r->d;
+            p.starts = d_start;
+            p.lens = d_len;
+            p.thrs = d_thr;
+            p.split_win = d_split;
+            p.n_split = (uint32_t)split.size();
+            p.next = ws.ctrl.as<uint32_t>();
+            p.out_pos = reinterpret_cast<unsigned long long *>(ws.ctrl.as<uint64_t>() + 1);
+            p.lists = ws.lists.as<uint64_t>();
+            p.list_cap = (uint32_t)list_cap;
+            p.lmfi = ws.lmfi.as<uint32_t>();
+            p.lmfi_cap = (uint32_t)lmfi_cap;
+            p.pool_m = ws.pool_m.as<uint64_t>();
+            p.pool_s = ws.pool_s.as<uint32_t>();
+            p.pool_cap = (uint32_t)pool_cap;
+            p.levels = ws.levels.ptr;
+            p.out_m = ws.out_m.as<uint64_t>();
+            p.out_s = ws.out_s.as<uint32_t>();
+            p.out_cap = out_cap;
+            // root records, then the task arrays (at most 128 tasks per window):
+            // win u32 | child u32 | order u32 | cnt u32 | kept u32 | status i32 | off u64 | nodes u64
+            const size_t roots_bytes = (n_windows * root_b + 255) & ~(size_t)255;
+            const size_t nt_max = n_windows * 128 + 1;
+            const size_t tsb = nt_max * (6 * 4 + 2 * 8) + 256;
+            ws.res.reserve(roots_bytes + tsb, st);
+            p.roots = ws.res.ptr;
+            // ---- 1. roots of the split windows
+            std::vector<unsigned char> roots_h;
+            if (!split.empty()) {
                 SG_CUDA_TRY(cudaEventRecord(k0, st));
-                launch_wmine(p, (int)mw, (unsigned)(use_warps / 4), st);
+                launch_wroot(p, (int)mw, (unsigned)std::min<uint64_t>((split.size() + 3) / 4, (uint64_t)h->n_sm * 8),
+                             st);
                 SG_CUDA_TRY(cudaEventRecord(k1, st));
                 ++launches;
                 ++h->launches;
-                SG_CUDA_TRY(cudaMemcpyAsync(ws.h_res.ptr, ws.res.ptr, rb, cudaMemcpyDeviceToHost, st));
+                roots_h.resize(n_windows * root_b);
+                SG_CUDA_TRY(cudaMemcpyAsync(roots_h.data(), ws.res.ptr, n_windows * root_b, cudaMemcpyDeviceToHost, st));
+                h->sync();
+                kernel_ms += timed_ms();
+            }
+            // root record fields (layout of WRoot<2>: hp[2], cand[2], cand_sup, has_cand, k, n, f[128], c[128])
+            auto root_at = [&](uint32_t w) { return roots_h.data() + (size_t)w * root_b; };
+            auto r_u32 = [&](uint32_t w, size_t off) {
+                uint32_t v;
+                memcpy(&v, root_at(w) + off, 4);
+                return v;
+            };
+            const size_t o_cand = 16, o_csup = 32, o_has = 36, o_k = 40, o_c = 176;
+            // ---- 2. tasks, costliest first
+            std::vector<uint32_t> t_win, t_child;
+            std::vector<double> t_cost;
+            std::vector<uint8_t> is_split(n_windows, 0);
+            for (uint32_t w : split) is_split[w] = 1;
+            for (uint64_t w = 0; w < n_windows; ++w) {
+                if (!is_split[w]) {
+                    t_win.push_back((uint32_t)w);
+                    t_child.push_back(kWholeWindow);
+                    t_cost.push_back(1300.0 * (double)lens[w]);
+                    continue;
+                }
+                if (r_u32((uint32_t)w, o_has)) {
+                    uint64_t m[2];
+                    memcpy(m, root_at((uint32_t)w) + o_cand, 16);
+                    root_cand.push_back(w);
+                    root_cand.push_back(m[0]);
+                    root_cand.push_back(m[1]);
+                    root_cand_sup.push_back(r_u32((uint32_t)w, o_csup));
+                    continue;
+                }
+                const uint32_t k = r_u32((uint32_t)w, o_k);
+                for (uint32_t j = 0; j < k; ++j) {
+                    t_win.push_back((uint32_t)w);
+                    t_child.push_back(j);
+                    t_cost.push_back((double)r_u32((uint32_t)w, o_c + 4 * j) * (double)(k - j));
+                }
+            }
+            const uint64_t nt = t_win.size();
+            n_tasks_total = nt;
+            std::vector<uint32_t> order(nt);
+            for (uint64_t i = 0; i < nt; ++i) order[i] = (uint32_t)i;
+            std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return t_cost[a] > t_cost[b]; });
+            const size_t nt1 = std::max<uint64_t>(nt, 1);
+            char *tb0 = ws.res.as<char>() + roots_bytes;
+            uint32_t *dt_win = reinterpret_cast<uint32_t *>(tb0);
+            uint32_t *dt_child = dt_win + nt1;
+            uint32_t *dt_order = dt_child + nt1;
+            uint32_t *dt_cnt = dt_order + nt1;
+            uint32_t *dt_kept = dt_cnt + nt1;
+            int32_t *dt_status = reinterpret_cast<int32_t *>(dt_kept + nt1);
+            uint64_t *dt_off = reinterpret_cast<uint64_t *>(tb0 + ((6 * 4 * nt1 + 15) & ~(size_t)15));
+            uint64_t *dt_nodes = dt_off + nt1;
+            d_task_off = dt_off;
+            d_task_cnt = dt_cnt;
+            ws.h_res.reserve(3 * nt1 * 4);
+            if (nt) {
+                uint32_t *hw = ws.h_res.as<uint32_t>();
+                memcpy(hw, t_win.data(), nt * 4);
+                memcpy(hw + nt1, t_child.data(), nt * 4);
+                memcpy(hw + 2 * nt1, order.data(), nt * 4);
+                SG_CUDA_TRY(cudaMemcpyAsync(dt_win, hw, 3 * nt1 * 4, cudaMemcpyHostToDevice, st));
+                p.task_win = dt_win;
+                p.task_child = dt_child;
+                p.task_order = dt_order;
+                p.n_tasks = (uint32_t)nt;
+                p.task_off = dt_off;
+                p.task_cnt = dt_cnt;
+                p.task_status = dt_status;
+                p.task_nodes = dt_nodes;
+                // ---- 3. all tasks in one persistent launch
+                const uint64_t use_warps = std::min<uint64_t>(warps, (nt + 3) & ~3ull);
+                SG_CUDA_TRY(cudaEventRecord(k0, st));
+                launch_wtask(p, (int)mw, (unsigned)(use_warps / 4), st);
+                SG_CUDA_TRY(cudaEventRecord(k1, st));
+                ++launches;
+                ++h->launches;
+                std::vector<uint32_t> cnt_h(nt), st_h(nt);
+                std::vector<uint64_t> nodes_h(nt);
+                SG_CUDA_TRY(cudaMemcpyAsync(cnt_h.data(), dt_cnt, nt * 4, cudaMemcpyDeviceToHost, st));
+                SG_CUDA_TRY(cudaMemcpyAsync(st_h.data(), dt_status, nt * 4, cudaMemcpyDeviceToHost, st));
+                SG_CUDA_TRY(cudaMemcpyAsync(nodes_h.data(), dt_nodes, nt * 8, cudaMemcpyDeviceToHost, st));
                 uint64_t used = 0;
                 SG_CUDA_TRY(cudaMemcpyAsync(&used, p.out_pos, 8, cudaMemcpyDeviceToHost, st));
                 h->sync();
-                float ms = 0.f;
-                SG_CUDA_TRY(cudaEventElapsedTime(&ms, k0, k1));
-                kernel_ms += ms;
+                kernel_ms += timed_ms();
                 used = std::min<uint64_t>(used, out_cap);
-                const uint64_t base = found_s.size();
-                found_m.resize((base + used) * mw);
-                found_s.resize(base + used);
-                if (used) {
-                    SG_CUDA_TRY(cudaMemcpyAsync(found_m.data() + base * mw, ws.out_m.ptr, used * mw * 8,
-                                                cudaMemcpyDeviceToHost, st));
-                    SG_CUDA_TRY(cudaMemcpyAsync(found_s.data() + base, ws.out_s.ptr, used * 4, cudaMemcpyDeviceToHost,
-                                                st));
-                    h->sync();
+                std::vector<uint8_t> bad(n_windows, 0);
+                for (uint64_t t = 0; t < nt; ++t) {
+                    nodes[t_win[t]] += nodes_h[t];
+                    if (st_h[t] != 0) bad[t_win[t]] = 1;
                 }
-                const uint64_t *h_off = ws.h_res.as<uint64_t>();
-                const uint64_t *h_nodes = h_off + n_windows;
-                const uint32_t *h_cnt = reinterpret_cast<const uint32_t *>(h_nodes + n_windows);
-                const int32_t *h_status = reinterpret_cast<const int32_t *>(h_cnt + n_windows);
-                std::vector<uint32_t> retry;
-                for (uint32_t w : pending) {
-                    if (h_status[w] == 0) {
-                        res_off[w] = base + h_off[w];
-                        res_cnt[w] = h_cnt[w];
-                        nodes[w] = h_nodes[w];
-                        batched[w] = 1;
-                    } else if (h_status[w] == 2) {
-                        retry.push_back(w);
-                    } else {
+                // ---- 4. cross-subtree filter of the split windows whose tasks all succeeded
+                std::vector<uint32_t> fwin, task0, task_of;
+                uint64_t max_m = 0;
+                {
+                    std::vector<uint64_t> first_task(n_windows, ~0ull);
+                    for (uint64_t t = 0; t < nt; ++t)
+                        if (first_task[t_win[t]] == ~0ull) first_task[t_win[t]] = t;
+                    for (uint32_t w : split) {
+                        if (bad[w] || first_task[w] == ~0ull) continue;
+                        const uint64_t f0 = first_task[w];
+                        uint64_t m = 0, t = f0;
+                        task0.push_back((uint32_t)task_of.size());
+                        for (; t < nt && t_win[t] == w; ++t) {
+                            task_of.push_back((uint32_t)t);   // tasks were created in subtree order
+                            m += cnt_h[t];
+                        }
+                        fwin.push_back(w);
+                        max_m = std::max(max_m, m);
+                    }
+                    task0.push_back((uint32_t)task_of.size());
+                }
+                kept.assign(cnt_h.begin(), cnt_h.end());
+                uint8_t *keep = reinterpret_cast<uint8_t *>(p.out_s + out_cap);
+                d_keep = keep;
+                if (!fwin.empty() && used) {
+                    SG_CUDA_TRY(cudaMemsetAsync(keep, 1, used, st));
+                    SG_CUDA_TRY(cudaMemcpyAsync(dt_kept, dt_cnt, nt * 4, cudaMemcpyDeviceToDevice, st));
+                    const uint64_t W = (max_m + 63) / 64;
+                    const uint64_t scratch_words = std::max<uint64_t>(W * r->d, 64);
+                    const uint64_t ctas = std::min<uint64_t>(fwin.size(), (uint64_t)h->n_sm * 2);
+                    // filter scratch and its tables share the lists buffer (the tasks are done with it)
+                    const size_t fb_tab = ((task0.size() + task_of.size()) * 4 + fwin.size() * 4 + 255) & ~(size_t)255;
+                    const size_t need = fb_tab + ctas * scratch_words * 8;
+                    ws.lists.reserve(need, st);
+                    char *fb = ws.lists.as<char>();
+                    uint32_t *d_task0 = reinterpret_cast<uint32_t *>(fb);
+                    uint32_t *d_task_of = d_task0 + task0.size();
+                    int32_t *d_wstat = reinterpret_cast<int32_t *>(d_task_of + task_of.size());
+                    std::vector<uint32_t> tabs(task0);
+                    tabs.insert(tabs.end(), task_of.begin(), task_of.end());
+                    SG_CUDA_TRY(cudaMemcpyAsync(d_task0, tabs.data(), tabs.size() * 4, cudaMemcpyHostToDevice, st));
+                    SG_CUDA_TRY(cudaMemsetAsync(d_wstat, 0, fwin.size() * 4, st));
+                    SG_CUDA_TRY(cudaMemsetAsync(ws.ctrl.as<uint32_t>() + 4, 0, 4, st));
+                    WFilterParams fp;
+                    fp.d = r->d;
+                    fp.n_win = (uint32_t)fwin.size();
+                    fp.win_task0 = d_task0;
+                    fp.task_of = d_task_of;
+                    fp.task_off = dt_off;
+                    fp.task_cnt = dt_cnt;
+                    fp.task_kept = dt_kept;
+                    fp.out_m = p.out_m;
+                    fp.keep = keep;
+                    fp.scratch = reinterpret_cast<uint64_t *>(fb + fb_tab);
+                    fp.scratch_words = scratch_words;
+                    fp.win_status = d_wstat;
+                    fp.next = ws.ctrl.as<uint32_t>() + 4;
+                    SG_CUDA_TRY(cudaEventRecord(k0, st));
+                    launch_wfilter(fp, (int)mw, (unsigned)ctas, st);
+                    SG_CUDA_TRY(cudaEventRecord(k1, st));
+                    ++launches;
+                    ++h->launches;
+                    std::vector<int32_t> wstat(fwin.size());
+                    SG_CUDA_TRY(cudaMemcpyAsync(kept.data(), dt_kept, nt * 4, cudaMemcpyDeviceToHost, st));
+                    SG_CUDA_TRY(cudaMemcpyAsync(wstat.data(), d_wstat, fwin.size() * 4, cudaMemcpyDeviceToHost, st));
+                    h->sync();
+                    kernel_ms += timed_ms();
+                    for (size_t i = 0; i < fwin.size(); ++i)
+                        if (wstat[i]) bad[fwin[i]] = 1;
+                } else {
+                    d_keep = nullptr;
+                }
+                t_win_of.assign(t_win.begin(), t_win.end());
+                for (uint64_t w = 0; w < n_windows; ++w) {
+                    if (bad[w]) {
                         wave.push_back(w);
+                        nodes[w] = 0;
                     }
                 }
-                if (retry.size() == pending.size()) {
-                    // nothing fitted the output arena: these go to the wave miner
-                    wave.insert(wave.end(), retry.begin(), retry.end());
-                    retry.clear();
-                }
-                pending.swap(retry);
+                for (uint64_t t = 0; t < nt; ++t)
+                    if (!bad[t_win[t]]) {
+                        res_cnt[t_win[t]] += kept[t];
+                        batched[t_win[t]] = 1;
+                    }
+                task_dst.assign(nt, ~0ull);
             }
+            for (size_t i = 0; i < root_cand_sup.size(); ++i) {
+                const uint64_t w = root_cand[3 * i];
+                res_cnt[w] = 1;
+                batched[w] = 1;
+            }
+            // split windows whose root has neither a candidate nor a frequent tail: empty
+            for (uint32_t w : split)
+                if (!r_u32(w, o_has) && r_u32(w, o_k) == 0) batched[w] = 1;
         } else {
             for (uint64_t w = 0; w < n_windows; ++w) wave.push_back(w);
         }
@@ -484,12 +642,13 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
         return fail(h, SGFIM_EDEVICE, e.what);
     }
 
-    // windows the batched kernel did not take: load and mine each on the handle
+    // windows the batched kernels did not take: load and mine each on the handle
     std::vector<uint64_t> wave_m;
     std::vector<uint32_t> wave_s;
     std::vector<uint64_t> wave_off(n_windows, 0);
     std::sort(wave.begin(), wave.end());
     for (uint64_t w : wave) {
+        batched[w] = 0;
         int rc = sgfim_ring_window_load(r, h, starts[w], lens[w]);
         sgfim_result *res = nullptr;
         if (rc == SGFIM_OK) {
@@ -539,18 +698,71 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
     uint64_t at = 0;
     for (uint64_t w = 0; w < n_windows; ++w) {
         R->offset[w] = at;
-        const uint64_t c = res_cnt[w];
-        if (c) {
-            // batched results exist only for rings of <= 128 items, where words == mw
-            const uint64_t *ms = batched[w] ? found_m.data() + res_off[w] * mw : wave_m.data() + wave_off[w] * words;
-            const uint32_t *ss = batched[w] ? found_s.data() + res_off[w] : wave_s.data() + wave_off[w];
-            memcpy(R->masks + at * words, ms, c * words * 8);
-            memcpy(R->support + at, ss, c * 4);
-        }
-        at += c;
+        at += res_cnt[w];
         R->status[w] = status[w];
         R->nodes[w] = nodes[w];
         R->batched[w] = batched[w];
+    }
+    // batched tasks: the device gathers the kept candidates into window order
+    try {
+        if (n_tasks_total && at) {
+            std::vector<uint64_t> fill(n_windows, 0);
+            uint64_t gathered = 0;
+            for (uint64_t t = 0; t < n_tasks_total; ++t) {
+                const uint64_t w = t_win_of[t];
+                if (!batched[w]) continue;
+                task_dst[t] = R->offset[w] + fill[w];
+                fill[w] += kept[t];
+                gathered += kept[t];
+            }
+            if (gathered) {
+                cudaStream_t st = h->stream;
+                WindowWorkspace &ws2 = h->wws;
+                // destination: the pool buffer (the tasks are done with it), masks then supports
+                const size_t need = at * mw * 8 + at * 4 + n_tasks_total * 8 + 512;
+                ws2.pool_m.reserve(need, st);
+                uint64_t *d_dst_m = ws2.pool_m.as<uint64_t>();
+                uint32_t *d_dst_s = reinterpret_cast<uint32_t *>(d_dst_m + at * mw);
+                uint64_t *d_task_dst = reinterpret_cast<uint64_t *>(
+                    (reinterpret_cast<uintptr_t>(d_dst_s + at) + 15) & ~(uintptr_t)15);
+                SG_CUDA_TRY(cudaMemcpyAsync(d_task_dst, task_dst.data(), n_tasks_total * 8, cudaMemcpyHostToDevice,
+                                            st));
+                WGatherParams gp;
+                gp.n_tasks = n_tasks_total;
+                gp.task_off = d_task_off;
+                gp.task_cnt = d_task_cnt;
+                gp.task_dst = d_task_dst;
+                gp.keep = d_keep;
+                gp.out_m = ws2.out_m.as<uint64_t>();
+                gp.out_s = ws2.out_s.as<uint32_t>();
+                gp.dst_m = d_dst_m;
+                gp.dst_s = d_dst_s;
+                launch_wgather(gp, (int)mw, (unsigned)std::min<uint64_t>((n_tasks_total + 3) / 4, (uint64_t)h->n_sm * 8),
+                               st);
+                ++launches;
+                ++h->launches;
+                SG_CUDA_TRY(cudaMemcpyAsync(R->masks, d_dst_m, at * mw * 8, cudaMemcpyDeviceToHost, st));
+                SG_CUDA_TRY(cudaMemcpyAsync(R->support, d_dst_s, at * 4, cudaMemcpyDeviceToHost, st));
+                h->sync();
+            }
+        }
+    } catch (const CudaError &e) {
+        sgfim_windows_result_free(R);
+        return fail(h, SGFIM_EDEVICE, e.what);
+    }
+    // terminal roots and wave-mined windows: host copies into their slots
+    for (size_t i = 0; i < root_cand_sup.size(); ++i) {
+        const uint64_t w = root_cand[3 * i];
+        if (!batched[w]) continue;
+        uint64_t *dstm = R->masks + R->offset[w] * words;
+        for (uint32_t k = 0; k < words; ++k) dstm[k] = k < 2 ? root_cand[3 * i + 1 + k] : 0;
+        R->support[R->offset[w]] = root_cand_sup[i];
+    }
+    for (uint64_t w : wave) {
+        const uint64_t c = res_cnt[w];
+        if (!c) continue;
+        memcpy(R->masks + R->offset[w] * words, wave_m.data() + wave_off[w] * words, c * words * 8);
+        memcpy(R->support + R->offset[w], wave_s.data() + wave_off[w], c * 4);
     }
     R->offset[n_windows] = at;
     R->elapsed_s = std::chrono::duration<double>(clk::now() - t0).count();

@@ -96,6 +96,11 @@ def test_ring_mine_windows_batched(engine):
         thrs[1] = 1
         thrs[3] = 1000          # above the window length
         thrs[5] = 1             # every distinct maximal transaction
+        # split windows (>= 4,096 transactions) at denser floors and a floor above the length
+        for L, thr in ((8192, 164), (8192, 82), (5000, 10 ** 6), (4096, 1)):
+            lens.append(L)
+            starts.append(head - L - int(rng.integers(0, (1 << 17) - L + 1)))
+            thrs.append(thr)
         res = ring.mine_windows(engine, starts, lens, thrs)
         assert len(res) == len(lens) and (res.status == 0).all()
         assert res.batched.all() and res.launches >= 1 and res.kernel_ms > 0

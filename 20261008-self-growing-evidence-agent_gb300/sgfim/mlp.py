@@ -136,10 +136,11 @@ class Trainer:
         hist = []
         for _ in range(epochs):
             perm = torch.randperm(n, generator=g).to(self.dev)
-            tot = 0.0
+            # the epoch's loss stays on the device: no host synchronisation per step
+            tot = torch.zeros(1, dtype=torch.float32, device=self.dev)
             for a in range(0, n, batch):
                 idx = perm[a:a + batch]
                 loss = self.step(Xd[idx], Yd[idx], Wd[idx] if Wd is not None else None, lr=lr)
-                tot += float(loss.item()) * len(idx)
-            hist.append(tot / n)
+                tot += loss * len(idx)
+            hist.append(float(tot.item()) / n)
         return hist

@@ -116,11 +116,18 @@ struct WMineParams {
     void *roots = nullptr;              // per window, wmine_root_bytes(MW) each
     const uint32_t *split_win = nullptr;
     uint32_t n_split = 0;
+    void *subs = nullptr;               // split root children, wmine_root_bytes(MW) each
+    const uint32_t *sub_win = nullptr;
+    const uint32_t *sub_child = nullptr;
+    uint32_t n_sub = 0;
     const uint32_t *task_win = nullptr;
     const uint32_t *task_child = nullptr;
+    const uint32_t *task_sub = nullptr;     // null or per task: split-child record, kWholeWindow = none
+    const uint32_t *task_gchild = nullptr;  // per task with a record: grandchild index, kWholeWindow = the
+                                            // record's own candidate (a terminal child)
     const uint32_t *task_order = nullptr;
     uint32_t n_tasks = 0;
-    uint32_t *next = nullptr;           // [0] task counter, [1] root counter
+    uint32_t *next = nullptr;           // [0] task counter, [1] root counter, [2] split-child counter
     uint64_t *lists = nullptr;
     uint32_t list_cap = 0;
     uint32_t *lmfi = nullptr;
@@ -139,12 +146,16 @@ struct WMineParams {
     uint64_t *task_nodes = nullptr;
 };
 // Cross-subtree maximality filter of split windows: window wi's tasks, in
-// subtree order, are task_of[win_task0[wi] .. win_task0[wi+1]).
+// depth-first subtree order, are entries win_task0[wi] .. win_task0[wi+1]-1
+// of task_of[]; task_first[entry] is the window-relative index of the task's
+// first candidate and win_total[wi] the window's candidate count.
 struct WFilterParams {
     uint32_t d = 0;
     uint32_t n_win = 0;
     const uint32_t *win_task0 = nullptr;
     const uint32_t *task_of = nullptr;
+    const uint64_t *task_first = nullptr;
+    const uint64_t *win_total = nullptr;
     const uint64_t *task_off = nullptr;
     const uint32_t *task_cnt = nullptr;
     uint32_t *task_kept = nullptr;      // in: task_cnt; out: kept
@@ -170,6 +181,7 @@ size_t wmine_level_bytes(int mw);
 size_t wmine_root_bytes(int mw);
 // blocks of 128 threads (4 warps; wfilter: 256 threads)
 void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
+void launch_wsub(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wgather(const WGatherParams &p, int mw, unsigned blocks, cudaStream_t st);

@@ -56,19 +56,19 @@ template <int MW> struct Mask {
 };
 
 template <int MW> __device__ __forceinline__ uint64_t m_word(const Mask<MW> &m, uint32_t i) {
+    // arithmetic selection: no indexable copy of m
     uint64_t r = 0;
 #pragma unroll
-    for (int k = 0; k < MW; ++k)
-        if ((uint32_t)k == i) r = m.w[k];
+    for (int k = 0; k < MW; ++k) r |= m.w[k] & (0ull - (uint64_t)((uint32_t)k == i));
     return r;
 }
 template <int MW> __device__ __forceinline__ bool m_has(const Mask<MW> &m, uint32_t e) {
     return (m_word(m, e >> 6) >> (e & 63)) & 1ull;
 }
 template <int MW> __device__ __forceinline__ void m_set(Mask<MW> &m, uint32_t e) {
+    const uint64_t bit = 1ull << (e & 63);
 #pragma unroll
-    for (int k = 0; k < MW; ++k)
-        if ((uint32_t)k == (e >> 6)) m.w[k] |= 1ull << (e & 63);
+    for (int k = 0; k < MW; ++k) m.w[k] |= bit & (0ull - (uint64_t)((uint32_t)k == (e >> 6)));
 }
 template <int MW> __device__ __forceinline__ bool m_nz(const Mask<MW> &m) {
     uint64_t x = 0;
@@ -134,22 +134,23 @@ template <int MW> struct alignas(16) WLevel {
     uint32_t c[128];        // supports of f
 };
 
-// Root of a split window (wroot_kernel -> wtask_kernel).
+// Root of a split window (wroot_kernel), or a root child that is split again
+// (wsub_kernel); read by wtask_kernel.
 template <int MW> struct alignas(16) WRoot {
     uint64_t hp[MW];        // root head after PEP (items in every transaction)
     uint64_t cand[MW];      // the window's only MFI when the root is terminal
     uint32_t cand_sup;
     uint32_t has_cand;      // 1: the MFI set is {cand}; 0: the tasks (k of them) hold it
     uint32_t k;
-    uint32_t n;             // window length
+    uint32_t overflow;      // subtree records: the node's database did not fit (mine the window elsewhere)
     uint8_t f[128];
     uint32_t c[128];
 };
 
 // the host reads these fields of the root records (ring.cu)
 static_assert(offsetof(WRoot<2>, cand) == 16 && offsetof(WRoot<2>, cand_sup) == 32 &&
-                  offsetof(WRoot<2>, has_cand) == 36 && offsetof(WRoot<2>, k) == 40 && offsetof(WRoot<2>, f) == 48 &&
-                  offsetof(WRoot<2>, c) == 176,
+                  offsetof(WRoot<2>, has_cand) == 36 && offsetof(WRoot<2>, k) == 40 &&
+                  offsetof(WRoot<2>, overflow) == 44 && offsetof(WRoot<2>, f) == 48 && offsetof(WRoot<2>, c) == 176,
               "root record layout read by sgfim_ring_mine_windows");
 
 // The search stack holds itemsets of up to kWDepth - 1 items.
@@ -269,12 +270,13 @@ __device__ __forceinline__ void sort_tail(const Mask<MW> &F, const uint32_t *cnt
     }
 }
 
-// Child database: entries holding e, restricted to Tc, non-empty, written at
-// dst .. dst+cn of the warp's stack.  Returns cn, or 0xffffffff on overflow.
+// Child database: entries holding every item of req, restricted to Tc,
+// non-empty, written at dst .. dst+cn of the warp's stack.  Returns cn, or
+// 0xffffffff on overflow.
 template <int MW>
 __device__ __forceinline__ uint32_t build_child(bool ring, const WMineParams &p, uint64_t start, uint64_t *lists,
-                                                uint64_t src_off, uint32_t src_n, uint32_t e, const Mask<MW> &Tc,
-                                                uint64_t dst, uint32_t lane) {
+                                                uint64_t src_off, uint32_t src_n, const Mask<MW> &req,
+                                                const Mask<MW> &Tc, uint64_t dst, uint32_t lane) {
     uint32_t cn = 0;
     for (uint32_t b = 0; b < src_n; b += 32 * kU) {
         Mask<MW> m[kU];
@@ -287,7 +289,7 @@ __device__ __forceinline__ uint32_t build_child(bool ring, const WMineParams &p,
             if (i < src_n) {
                 const Mask<MW> r = m_load<MW>(entry_ptr<MW>(ring, p, start, lists, src_off, i));
                 m[u] = m_and(r, Tc);
-                keep[u] = m_has(r, e) && m_nz(m[u]);
+                keep[u] = m_sub(req, r) && m_nz(m[u]);
             }
         }
         // the child's entries go after the source's: writes never touch entries still to be read
@@ -352,7 +354,87 @@ template <int MW> __global__ void __launch_bounds__(128) wroot_kernel(WMineParam
             R.cand_sup = csup;
             R.has_cand = has;
             R.k = has ? 0 : k;
-            R.n = n;
+            R.overflow = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ split root children
+// Child j of a split window's root, expanded like a root: its database is
+// built from the ring (transactions holding f_j, restricted to f_{j+1..}),
+// then counts, PEP, FHUT and the sorted frequent tail go to its record.
+template <int MW> __global__ void __launch_bounds__(128) wsub_kernel(WMineParams p) {
+    __shared__ uint32_t s_cnt[4][128];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint64_t warp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    uint32_t *cnt = s_cnt[wib];
+    uint64_t *lists = p.lists + warp * (uint64_t)p.list_cap * MW;
+    const WRoot<MW> *roots = reinterpret_cast<const WRoot<MW> *>(p.roots);
+    WRoot<MW> *subs = reinterpret_cast<WRoot<MW> *>(p.subs);
+    for (;;) {
+        uint32_t si = 0;
+        if (lane == 0) si = atomicAdd(p.next + 2, 1u);
+        si = __shfl_sync(kFull, si, 0);
+        if (si >= p.n_sub) break;
+        const uint32_t w = p.sub_win[si], j = p.sub_child[si];
+        const uint64_t start = p.starts[w];
+        const uint32_t n = p.lens[w];
+        const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
+        const WRoot<MW> &R = roots[w];
+        const uint32_t k = R.k;
+        Mask<MW> T = m_zero<MW>(), req = m_zero<MW>();
+        for (uint32_t q = j + 1 + lane; q < k; q += 32) m_set(T, R.f[q]);
+        T = warp_or(T);
+        const uint32_t e = R.f[j];
+        m_set(req, e);
+        Mask<MW> H = m_load<MW>(R.hp);
+        m_set(H, e);
+        const uint32_t sup = R.c[j];
+        WRoot<MW> &S = subs[si];
+        uint32_t n1 = 0, overflow = 0;
+        if (m_nz(T)) {
+            n1 = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+            if (n1 == 0xffffffffu) {
+                overflow = 1;
+                n1 = 0;
+            }
+        }
+        count_items<MW>(false, p, start, lists, 0, n1, T, cnt, lane);
+        Mask<MW> P, F;
+        classify<MW>(T, cnt, p.d, thr, sup, lane, P, F);
+        uint32_t k1 = 0;
+        Mask<MW> Hp, cand;
+#pragma unroll
+        for (int i = 0; i < MW; ++i) {
+            Hp.w[i] = H.w[i] | P.w[i];
+            cand.w[i] = Hp.w[i];
+            k1 += __popcll(F.w[i]);
+        }
+        uint32_t has = 0, csup = 0;
+        if (k1 == 0) {
+            has = 1;   // Hp holds f_j
+            csup = sup;
+        } else {
+            const uint32_t cf = count_superset<MW>(false, p, start, lists, 0, n1, F, lane);
+            if (cf >= thr) {
+                has = 1;
+                csup = cf;
+#pragma unroll
+                for (int i = 0; i < MW; ++i) cand.w[i] |= F.w[i];
+            }
+        }
+        if (!has) sort_tail<MW>(F, cnt, lane, S.f, S.c);
+        if (lane < MW) {
+            S.hp[lane] = m_word(Hp, lane);
+            S.cand[lane] = m_word(cand, lane);
+        }
+        if (lane == 0) {
+            S.cand_sup = csup;
+            S.has_cand = has;
+            S.k = has ? 0 : k1;
+            S.overflow = overflow;
         }
         __syncwarp();
     }
@@ -381,6 +463,8 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
         const uint32_t t = p.task_order[ti];
         const uint32_t w = p.task_win[t];
         const uint32_t child = p.task_child[t];
+        const uint32_t sub = p.task_sub ? p.task_sub[t] : kWholeWindow;
+        const uint32_t gchild = p.task_gchild ? p.task_gchild[t] : kWholeWindow;
         const uint64_t start = p.starts[w];
         const uint32_t n = p.lens[w];
         const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
@@ -392,21 +476,49 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
         bool ring0 = child == kWholeWindow;
         Mask<MW> H = m_zero<MW>(), T = m_zero<MW>();
         uint32_t sup = n, list_n = n;
+        bool done = false;   // a split child that is itself terminal: its one candidate
         if (ring0) {
             for (uint32_t e = 0; e < d; ++e) m_set(T, e);
-        } else {
+        } else if (sub == kWholeWindow) {
             const WRoot<MW> &R = roots[w];
             const uint32_t k = R.k;
             for (uint32_t q = child + 1 + lane; q < k; q += 32) m_set(T, R.f[q]);
             T = warp_or(T);
             H = m_load<MW>(R.hp);
-            const uint32_t e = R.f[child];
-            m_set(H, e);
+            Mask<MW> req = m_zero<MW>();
+            m_set(req, R.f[child]);
+            m_set(H, R.f[child]);
             sup = R.c[child];
             list_n = 0;
             if (m_nz(T)) {
-                list_n = build_child<MW>(true, p, start, lists, 0, n, e, T, 0, lane);
+                list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
                 if (list_n == 0xffffffffu) status = 1;
+            }
+        } else {
+            const WRoot<MW> &S = reinterpret_cast<const WRoot<MW> *>(p.subs)[sub];
+            if (S.overflow) {
+                status = 1;
+            } else if (gchild == kWholeWindow) {
+                if (lane < MW) pool[lane] = S.cand[lane];
+                if (lane == 0) pool_s[0] = S.cand_sup;
+                np = 1;
+                nodes = 1;
+                done = true;
+            } else {
+                const uint32_t k1 = S.k;
+                for (uint32_t q = gchild + 1 + lane; q < k1; q += 32) m_set(T, S.f[q]);
+                T = warp_or(T);
+                H = m_load<MW>(S.hp);
+                Mask<MW> req = m_zero<MW>();
+                m_set(req, roots[w].f[child]);
+                m_set(req, S.f[gchild]);
+                m_set(H, S.f[gchild]);
+                sup = S.c[gchild];
+                list_n = 0;
+                if (m_nz(T)) {
+                    list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+                    if (list_n == 0xffffffffu) status = 1;
+                }
             }
         }
         int l = 0;
@@ -414,7 +526,7 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
         uint32_t lm_off = 0, lm_n = 0, entry = 0;
         bool expand = true;
 
-        while (status == 0) {
+        while (status == 0 && !done) {
             if (expand) {
                 expand = false;
                 ++nodes;
@@ -507,7 +619,9 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
             const uint64_t c_off = pring ? 0 : p_off + p_n;
             uint32_t cn = 0;
             if (m_nz(Tc)) {
-                cn = build_child<MW>(pring, p, start, lists, p_off, p_n, e, Tc, c_off, lane);
+                Mask<MW> req = m_zero<MW>();
+                m_set(req, e);
+                cn = build_child<MW>(pring, p, start, lists, p_off, p_n, req, Tc, c_off, lane);
                 if (cn == 0xffffffffu) { status = 1; break; }
             }
             // child local-MFI list: members containing the child's head
@@ -576,12 +690,11 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
 }
 
 // ------------------------------------------------------------------ cross-task filter
-// One CTA per split window: the window's candidates in task order (subtree
-// j ascending) get a vertical bitmap rows[e][p]; candidate p of subtree j is
-// dropped when the AND of its items' rows has a bit below the first
-// candidate of subtree j.  keep[] is written per arena slot, kept[] per task.
+// One CTA per split window: the window's candidates in task order (subtrees
+// in depth-first order) get a vertical bitmap rows[e][q]; candidate q of a
+// task is dropped when the AND of its items' rows has a bit below the task's
+// first candidate.  keep[] is written per arena slot, kept[] per task.
 template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterParams p) {
-    __shared__ uint64_t s_first[129];    // first candidate (window order) of each task, + total
     __shared__ uint32_t s_w;
     uint64_t *rows = p.scratch + (uint64_t)blockIdx.x * p.scratch_words;
     for (;;) {
@@ -590,17 +703,8 @@ template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterP
         __syncthreads();
         const uint32_t wi = s_w;
         if (wi >= p.n_win) break;
-        const uint32_t t0 = p.win_task0[wi], nt = p.win_task0[wi + 1] - t0;   // tasks of this window, j order
-        if (threadIdx.x == 0) {
-            uint64_t acc = 0;
-            for (uint32_t j = 0; j < nt; ++j) {
-                s_first[j] = acc;
-                acc += p.task_cnt[p.task_of[t0 + j]];
-            }
-            s_first[nt] = acc;
-        }
-        __syncthreads();
-        const uint64_t M = s_first[nt];
+        const uint32_t e0 = p.win_task0[wi], e1 = p.win_task0[wi + 1];   // entries of this window, task order
+        const uint64_t M = p.win_total[wi];
         const uint64_t W = (M + 63) / 64;
         if (W * p.d > p.scratch_words) {
             if (threadIdx.x == 0) p.win_status[wi] = 1;
@@ -608,11 +712,19 @@ template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterP
         }
         for (uint64_t i = threadIdx.x; i < W * p.d; i += blockDim.x) rows[i] = 0;
         __syncthreads();
-        // candidate q (window order) -> task j, arena slot
+        // candidate q (window order) -> entry (binary search over first[]), arena slot
+        auto locate = [&](uint64_t q) {
+            uint32_t lo = e0, hi = e1 - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (p.task_first[mid] <= q) lo = mid;
+                else hi = mid - 1;
+            }
+            return lo;
+        };
         for (uint64_t q = threadIdx.x; q < M; q += blockDim.x) {
-            uint32_t j = 0;
-            while (s_first[j + 1] <= q) ++j;
-            const uint64_t slot = p.task_off[p.task_of[t0 + j]] + (q - s_first[j]);
+            const uint32_t en = locate(q);
+            const uint64_t slot = p.task_off[p.task_of[en]] + (q - p.task_first[en]);
             const Mask<MW> m = m_load<MW>(p.out_m + slot * MW);
 #pragma unroll
             for (int ww = 0; ww < MW; ++ww) {
@@ -627,19 +739,19 @@ template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterP
         }
         __syncthreads();
         for (uint64_t q = threadIdx.x; q < M; q += blockDim.x) {
-            uint32_t j = 0;
-            while (s_first[j + 1] <= q) ++j;
-            const uint32_t t = p.task_of[t0 + j];
-            const uint64_t slot = p.task_off[t] + (q - s_first[j]);
+            const uint32_t en = locate(q);
+            const uint32_t t = p.task_of[en];
+            const uint64_t slot = p.task_off[t] + (q - p.task_first[en]);
             bool keep = true;
-            const uint64_t lim = s_first[j];   // candidates of earlier subtrees: [0, lim)
+            const uint64_t lim = p.task_first[en];   // candidates of earlier subtrees: [0, lim)
             if (lim) {
                 const Mask<MW> m = m_load<MW>(p.out_m + slot * MW);
-                uint32_t e0 = 0;
-                for (int ww = 0; ww < MW; ++ww)
-                    if (m.w[ww]) { e0 = ww * 64 + (__ffsll((long long)m.w[ww]) - 1); break; }
+                uint32_t ef = 0;
+#pragma unroll
+                for (int ww = MW - 1; ww >= 0; --ww)
+                    if (m.w[ww]) ef = ww * 64 + (__ffsll((long long)m.w[ww]) - 1);
                 for (uint64_t wd = 0; wd * 64 < lim && keep; ++wd) {
-                    uint64_t v = rows[(uint64_t)e0 * W + wd];
+                    uint64_t v = rows[(uint64_t)ef * W + wd];
                     if (wd * 64 + 64 > lim) v &= (1ull << (lim - wd * 64)) - 1;
 #pragma unroll
                     for (int ww = 0; ww < MW; ++ww) {
@@ -690,6 +802,11 @@ size_t wmine_root_bytes(int mw) { return mw == 2 ? sizeof(WRoot<2>) : 0; }
 void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
     if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
     wroot_kernel<2><<<blocks, 128, 0, st>>>(p);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+void launch_wsub(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
+    if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
+    wsub_kernel<2><<<blocks, 128, 0, st>>>(p);
     SG_CUDA_TRY(cudaGetLastError());
 }
 void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {

@@ -375,6 +375,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             ws.out_m.reserve(out_cap * mw * 8, st);
             ws.out_s.reserve(out_cap * 5, st);   // supports, then the keep flags
             ws.ctrl.reserve(256, st);
+            ws.res.reserve(n_windows * root_b, st);
             // window table: starts u64 | lens u32 | thrs u32 | split u32
             const size_t tb = n_windows * 8 + 3 * n_windows * 4;
             ws.table.reserve(tb, st);
@@ -415,10 +416,11 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             p.starts = d_start;
             p.lens = d_len;
             p.thrs = d_thr;
+            p.roots = ws.res.ptr;
             p.split_win = d_split;
             p.n_split = (uint32_t)split.size();
             p.next = ws.ctrl.as<uint32_t>();
-            p.out_pos = reinterpret_cast<unsigned long long *>(ws.ctrl.as<uint64_t>() + 1);
+            p.out_pos = reinterpret_cast<unsigned long long *>(ws.ctrl.as<uint64_t>() + 2);
             p.lists = ws.lists.as<uint64_t>();
             p.list_cap = (uint32_t)list_cap;
             p.lmfi = ws.lmfi.as<uint32_t>();
@@ -430,13 +432,13 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             p.out_m = ws.out_m.as<uint64_t>();
             p.out_s = ws.out_s.as<uint32_t>();
             p.out_cap = out_cap;
-            // root records, then the task arrays (at most 128 tasks per window):
-            // win u32 | child u32 | order u32 | cnt u32 | kept u32 | status i32 | off u64 | nodes u64
-            const size_t roots_bytes = (n_windows * root_b + 255) & ~(size_t)255;
-            const size_t nt_max = n_windows * 128 + 1;
-            const size_t tsb = nt_max * (6 * 4 + 2 * 8) + 256;
-            ws.res.reserve(roots_bytes + tsb, st);
-            p.roots = ws.res.ptr;
+            // record fields read here (WRoot<2>: hp[2], cand[2], cand_sup, has_cand, k, overflow, f[128], c[128])
+            const size_t o_cand = 16, o_csup = 32, o_has = 36, o_k = 40, o_ovf = 44, o_f = 48, o_c = 176;
+            auto u32_at = [](const unsigned char *rec, size_t off) {
+                uint32_t v;
+                memcpy(&v, rec + off, 4);
+                return v;
+            };
             // ---- 1. roots of the split windows
             std::vector<unsigned char> roots_h;
             if (!split.empty()) {
@@ -451,75 +453,144 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 h->sync();
                 kernel_ms += timed_ms();
             }
-            // root record fields (layout of WRoot<2>: hp[2], cand[2], cand_sup, has_cand, k, n, f[128], c[128])
-            auto root_at = [&](uint32_t w) { return roots_h.data() + (size_t)w * root_b; };
-            auto r_u32 = [&](uint32_t w, size_t off) {
-                uint32_t v;
-                memcpy(&v, root_at(w) + off, 4);
-                return v;
-            };
-            const size_t o_cand = 16, o_csup = 32, o_has = 36, o_k = 40, o_c = 176;
-            // ---- 2. tasks, costliest first
-            std::vector<uint32_t> t_win, t_child;
-            std::vector<double> t_cost;
-            std::vector<uint8_t> is_split(n_windows, 0);
+            auto root_at = [&](uint64_t w) { return roots_h.data() + (size_t)w * root_b; };
+            std::vector<uint8_t> is_split(n_windows, 0), bad(n_windows, 0);
             for (uint32_t w : split) is_split[w] = 1;
+            // ---- 2. the costliest root children are split again (their own expansion in wsub_kernel)
+            double total_cost = 0.0;
             for (uint64_t w = 0; w < n_windows; ++w) {
                 if (!is_split[w]) {
-                    t_win.push_back((uint32_t)w);
-                    t_child.push_back(kWholeWindow);
-                    t_cost.push_back(1300.0 * (double)lens[w]);
+                    total_cost += 1300.0 * (double)lens[w];
                     continue;
                 }
-                if (r_u32((uint32_t)w, o_has)) {
+                const unsigned char *R = root_at(w);
+                const uint32_t k = u32_at(R, o_has) ? 0 : u32_at(R, o_k);
+                for (uint32_t j = 0; j < k; ++j) total_cost += (double)u32_at(R, o_c + 4 * j) * (double)(k - j);
+            }
+            const double split_above = total_cost / (double)(warps * 2);
+            std::vector<uint32_t> sub_win, sub_child;
+            std::vector<uint32_t> sub_of_first(n_windows, 0);   // first sub index of each split window
+            for (uint32_t w : split) {
+                sub_of_first[w] = (uint32_t)sub_win.size();
+                const unsigned char *R = root_at(w);
+                if (u32_at(R, o_has)) continue;
+                const uint32_t k = u32_at(R, o_k);
+                for (uint32_t j = 0; j + 2 < k; ++j)
+                    if ((double)u32_at(R, o_c + 4 * j) * (double)(k - j) > split_above) {
+                        sub_win.push_back(w);
+                        sub_child.push_back(j);
+                    }
+            }
+            std::vector<unsigned char> subs_h;
+            if (!sub_win.empty()) {
+                const size_t ns = sub_win.size();
+                ws.sub.reserve(ns * root_b + ns * 8 + 256, st);
+                uint32_t *d_sw = reinterpret_cast<uint32_t *>(ws.sub.as<char>() + ((ns * root_b + 255) & ~(size_t)255));
+                std::vector<uint32_t> sw(sub_win);
+                sw.insert(sw.end(), sub_child.begin(), sub_child.end());
+                SG_CUDA_TRY(cudaMemcpyAsync(d_sw, sw.data(), sw.size() * 4, cudaMemcpyHostToDevice, st));
+                p.subs = ws.sub.ptr;
+                p.sub_win = d_sw;
+                p.sub_child = d_sw + ns;
+                p.n_sub = (uint32_t)ns;
+                SG_CUDA_TRY(cudaEventRecord(k0, st));
+                launch_wsub(p, (int)mw, (unsigned)(std::min<uint64_t>(warps, (ns + 3) & ~3ull) / 4), st);
+                SG_CUDA_TRY(cudaEventRecord(k1, st));
+                ++launches;
+                ++h->launches;
+                subs_h.resize(ns * root_b);
+                SG_CUDA_TRY(cudaMemcpyAsync(subs_h.data(), ws.sub.ptr, ns * root_b, cudaMemcpyDeviceToHost, st));
+                h->sync();
+                kernel_ms += timed_ms();
+            }
+            // ---- 3. tasks in depth-first order within each window
+            std::vector<uint32_t> t_win, t_child, t_sub, t_gchild;
+            std::vector<double> t_cost;
+            auto add_task = [&](uint32_t w, uint32_t c, uint32_t sb, uint32_t g, double cost) {
+                t_win.push_back(w);
+                t_child.push_back(c);
+                t_sub.push_back(sb);
+                t_gchild.push_back(g);
+                t_cost.push_back(cost);
+            };
+            for (uint64_t w = 0; w < n_windows; ++w) {
+                if (!is_split[w]) {
+                    add_task((uint32_t)w, kWholeWindow, kWholeWindow, kWholeWindow, 1300.0 * (double)lens[w]);
+                    continue;
+                }
+                const unsigned char *R = root_at(w);
+                if (u32_at(R, o_has)) {
                     uint64_t m[2];
-                    memcpy(m, root_at((uint32_t)w) + o_cand, 16);
+                    memcpy(m, R + o_cand, 16);
                     root_cand.push_back(w);
                     root_cand.push_back(m[0]);
                     root_cand.push_back(m[1]);
-                    root_cand_sup.push_back(r_u32((uint32_t)w, o_csup));
+                    root_cand_sup.push_back(u32_at(R, o_csup));
                     continue;
                 }
-                const uint32_t k = r_u32((uint32_t)w, o_k);
+                const uint32_t k = u32_at(R, o_k);
+                uint32_t si = sub_of_first[w];
                 for (uint32_t j = 0; j < k; ++j) {
-                    t_win.push_back((uint32_t)w);
-                    t_child.push_back(j);
-                    t_cost.push_back((double)r_u32((uint32_t)w, o_c + 4 * j) * (double)(k - j));
+                    if (si < sub_win.size() && sub_win[si] == w && sub_child[si] == j) {
+                        const unsigned char *S = subs_h.data() + (size_t)si * root_b;
+                        if (u32_at(S, o_ovf)) {
+                            bad[w] = 1;
+                        } else if (u32_at(S, o_has)) {
+                            add_task((uint32_t)w, j, si, kWholeWindow, 1.0);
+                        } else {
+                            const uint32_t k1 = u32_at(S, o_k);
+                            for (uint32_t g = 0; g < k1; ++g)
+                                add_task((uint32_t)w, j, si, g, (double)u32_at(S, o_c + 4 * g) * (double)(k1 - g));
+                        }
+                        ++si;
+                    } else {
+                        add_task((uint32_t)w, j, kWholeWindow, kWholeWindow,
+                                 (double)u32_at(R, o_c + 4 * j) * (double)(k - j));
+                    }
                 }
             }
+            (void)o_f;
             const uint64_t nt = t_win.size();
             n_tasks_total = nt;
             std::vector<uint32_t> order(nt);
             for (uint64_t i = 0; i < nt; ++i) order[i] = (uint32_t)i;
-            std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return t_cost[a] > t_cost[b]; });
+            std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return t_cost[x] > t_cost[y]; });
+            // task arrays: win | child | sub | gchild | order | cnt | kept | status (u32) | off | nodes (u64)
             const size_t nt1 = std::max<uint64_t>(nt, 1);
-            char *tb0 = ws.res.as<char>() + roots_bytes;
-            uint32_t *dt_win = reinterpret_cast<uint32_t *>(tb0);
+            const size_t u32_bytes = (8 * 4 * nt1 + 15) & ~(size_t)15;
+            ws.tasks.reserve(u32_bytes + 2 * 8 * nt1, st);
+            uint32_t *dt_win = ws.tasks.as<uint32_t>();
             uint32_t *dt_child = dt_win + nt1;
-            uint32_t *dt_order = dt_child + nt1;
+            uint32_t *dt_sub = dt_child + nt1;
+            uint32_t *dt_gchild = dt_sub + nt1;
+            uint32_t *dt_order = dt_gchild + nt1;
             uint32_t *dt_cnt = dt_order + nt1;
             uint32_t *dt_kept = dt_cnt + nt1;
             int32_t *dt_status = reinterpret_cast<int32_t *>(dt_kept + nt1);
-            uint64_t *dt_off = reinterpret_cast<uint64_t *>(tb0 + ((6 * 4 * nt1 + 15) & ~(size_t)15));
+            uint64_t *dt_off = reinterpret_cast<uint64_t *>(ws.tasks.as<char>() + u32_bytes);
             uint64_t *dt_nodes = dt_off + nt1;
             d_task_off = dt_off;
             d_task_cnt = dt_cnt;
-            ws.h_res.reserve(3 * nt1 * 4);
             if (nt) {
+                ws.h_res.reserve(5 * nt1 * 4);
                 uint32_t *hw = ws.h_res.as<uint32_t>();
                 memcpy(hw, t_win.data(), nt * 4);
                 memcpy(hw + nt1, t_child.data(), nt * 4);
-                memcpy(hw + 2 * nt1, order.data(), nt * 4);
-                SG_CUDA_TRY(cudaMemcpyAsync(dt_win, hw, 3 * nt1 * 4, cudaMemcpyHostToDevice, st));
+                memcpy(hw + 2 * nt1, t_sub.data(), nt * 4);
+                memcpy(hw + 3 * nt1, t_gchild.data(), nt * 4);
+                memcpy(hw + 4 * nt1, order.data(), nt * 4);
+                SG_CUDA_TRY(cudaMemcpyAsync(dt_win, hw, 5 * nt1 * 4, cudaMemcpyHostToDevice, st));
                 p.task_win = dt_win;
                 p.task_child = dt_child;
+                p.task_sub = dt_sub;
+                p.task_gchild = dt_gchild;
                 p.task_order = dt_order;
                 p.n_tasks = (uint32_t)nt;
                 p.task_off = dt_off;
                 p.task_cnt = dt_cnt;
                 p.task_status = dt_status;
                 p.task_nodes = dt_nodes;
-                // ---- 3. all tasks in one persistent launch
+                // ---- 4. all tasks in one persistent launch
                 const uint64_t use_warps = std::min<uint64_t>(warps, (nt + 3) & ~3ull);
                 SG_CUDA_TRY(cudaEventRecord(k0, st));
                 launch_wtask(p, (int)mw, (unsigned)(use_warps / 4), st);
@@ -536,68 +607,77 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 h->sync();
                 kernel_ms += timed_ms();
                 used = std::min<uint64_t>(used, out_cap);
-                std::vector<uint8_t> bad(n_windows, 0);
                 for (uint64_t t = 0; t < nt; ++t) {
                     nodes[t_win[t]] += nodes_h[t];
                     if (st_h[t] != 0) bad[t_win[t]] = 1;
                 }
-                // ---- 4. cross-subtree filter of the split windows whose tasks all succeeded
+                // ---- 5. cross-subtree filter of the split windows whose tasks all succeeded
                 std::vector<uint32_t> fwin, task0, task_of;
+                std::vector<uint64_t> first, wtotal;
                 uint64_t max_m = 0;
-                {
-                    std::vector<uint64_t> first_task(n_windows, ~0ull);
-                    for (uint64_t t = 0; t < nt; ++t)
-                        if (first_task[t_win[t]] == ~0ull) first_task[t_win[t]] = t;
-                    for (uint32_t w : split) {
-                        if (bad[w] || first_task[w] == ~0ull) continue;
-                        const uint64_t f0 = first_task[w];
-                        uint64_t m = 0, t = f0;
+                for (uint64_t t = 0; t < nt;) {
+                    const uint32_t w = t_win[t];
+                    uint64_t t2 = t;
+                    while (t2 < nt && t_win[t2] == w) ++t2;
+                    if (is_split[w] && !bad[w]) {
                         task0.push_back((uint32_t)task_of.size());
-                        for (; t < nt && t_win[t] == w; ++t) {
-                            task_of.push_back((uint32_t)t);   // tasks were created in subtree order
-                            m += cnt_h[t];
+                        uint64_t m = 0;
+                        for (uint64_t x = t; x < t2; ++x) {
+                            task_of.push_back((uint32_t)x);   // tasks were created in depth-first order
+                            first.push_back(m);
+                            m += cnt_h[x];
                         }
                         fwin.push_back(w);
+                        wtotal.push_back(m);
                         max_m = std::max(max_m, m);
                     }
-                    task0.push_back((uint32_t)task_of.size());
+                    t = t2;
                 }
+                task0.push_back((uint32_t)task_of.size());
                 kept.assign(cnt_h.begin(), cnt_h.end());
                 uint8_t *keep = reinterpret_cast<uint8_t *>(p.out_s + out_cap);
-                d_keep = keep;
+                d_keep = nullptr;
                 if (!fwin.empty() && used) {
+                    d_keep = keep;
                     SG_CUDA_TRY(cudaMemsetAsync(keep, 1, used, st));
                     SG_CUDA_TRY(cudaMemcpyAsync(dt_kept, dt_cnt, nt * 4, cudaMemcpyDeviceToDevice, st));
                     const uint64_t W = (max_m + 63) / 64;
                     const uint64_t scratch_words = std::max<uint64_t>(W * r->d, 64);
                     const uint64_t ctas = std::min<uint64_t>(fwin.size(), (uint64_t)h->n_sm * 2);
-                    // filter scratch and its tables share the lists buffer (the tasks are done with it)
-                    const size_t fb_tab = ((task0.size() + task_of.size()) * 4 + fwin.size() * 4 + 255) & ~(size_t)255;
-                    const size_t need = fb_tab + ctas * scratch_words * 8;
-                    ws.lists.reserve(need, st);
+                    // tables: first u64 | total u64 | task0 u32 | task_of u32 | status i32, then the scratch
+                    const size_t tab =
+                        ((first.size() + wtotal.size()) * 8 + (task0.size() + task_of.size() + fwin.size()) * 4 + 255) &
+                        ~(size_t)255;
+                    ws.lists.reserve(tab + ctas * scratch_words * 8, st);
                     char *fb = ws.lists.as<char>();
-                    uint32_t *d_task0 = reinterpret_cast<uint32_t *>(fb);
+                    uint64_t *d_first = reinterpret_cast<uint64_t *>(fb);
+                    uint64_t *d_total = d_first + first.size();
+                    uint32_t *d_task0 = reinterpret_cast<uint32_t *>(d_total + wtotal.size());
                     uint32_t *d_task_of = d_task0 + task0.size();
                     int32_t *d_wstat = reinterpret_cast<int32_t *>(d_task_of + task_of.size());
-                    std::vector<uint32_t> tabs(task0);
-                    tabs.insert(tabs.end(), task_of.begin(), task_of.end());
-                    SG_CUDA_TRY(cudaMemcpyAsync(d_task0, tabs.data(), tabs.size() * 4, cudaMemcpyHostToDevice, st));
+                    std::vector<uint64_t> t64(first);
+                    t64.insert(t64.end(), wtotal.begin(), wtotal.end());
+                    std::vector<uint32_t> t32(task0);
+                    t32.insert(t32.end(), task_of.begin(), task_of.end());
+                    SG_CUDA_TRY(cudaMemcpyAsync(d_first, t64.data(), t64.size() * 8, cudaMemcpyHostToDevice, st));
+                    SG_CUDA_TRY(cudaMemcpyAsync(d_task0, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice, st));
                     SG_CUDA_TRY(cudaMemsetAsync(d_wstat, 0, fwin.size() * 4, st));
-                    SG_CUDA_TRY(cudaMemsetAsync(ws.ctrl.as<uint32_t>() + 4, 0, 4, st));
                     WFilterParams fp;
                     fp.d = r->d;
                     fp.n_win = (uint32_t)fwin.size();
                     fp.win_task0 = d_task0;
                     fp.task_of = d_task_of;
+                    fp.task_first = d_first;
+                    fp.win_total = d_total;
                     fp.task_off = dt_off;
                     fp.task_cnt = dt_cnt;
                     fp.task_kept = dt_kept;
                     fp.out_m = p.out_m;
                     fp.keep = keep;
-                    fp.scratch = reinterpret_cast<uint64_t *>(fb + fb_tab);
+                    fp.scratch = reinterpret_cast<uint64_t *>(fb + tab);
                     fp.scratch_words = scratch_words;
                     fp.win_status = d_wstat;
-                    fp.next = ws.ctrl.as<uint32_t>() + 4;
+                    fp.next = ws.ctrl.as<uint32_t>() + 8;
                     SG_CUDA_TRY(cudaEventRecord(k0, st));
                     launch_wfilter(fp, (int)mw, (unsigned)ctas, st);
                     SG_CUDA_TRY(cudaEventRecord(k1, st));
@@ -610,16 +690,8 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                     kernel_ms += timed_ms();
                     for (size_t i = 0; i < fwin.size(); ++i)
                         if (wstat[i]) bad[fwin[i]] = 1;
-                } else {
-                    d_keep = nullptr;
                 }
                 t_win_of.assign(t_win.begin(), t_win.end());
-                for (uint64_t w = 0; w < n_windows; ++w) {
-                    if (bad[w]) {
-                        wave.push_back(w);
-                        nodes[w] = 0;
-                    }
-                }
                 for (uint64_t t = 0; t < nt; ++t)
                     if (!bad[t_win[t]]) {
                         res_cnt[t_win[t]] += kept[t];
@@ -633,8 +705,17 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 batched[w] = 1;
             }
             // split windows whose root has neither a candidate nor a frequent tail: empty
-            for (uint32_t w : split)
-                if (!r_u32(w, o_has) && r_u32(w, o_k) == 0) batched[w] = 1;
+            for (uint32_t w : split) {
+                const unsigned char *R = root_at(w);
+                if (!u32_at(R, o_has) && u32_at(R, o_k) == 0) batched[w] = 1;
+            }
+            for (uint64_t w = 0; w < n_windows; ++w)
+                if (bad[w]) {
+                    batched[w] = 0;
+                    res_cnt[w] = 0;
+                    nodes[w] = 0;
+                    wave.push_back(w);
+                }
         } else {
             for (uint64_t w = 0; w < n_windows; ++w) wave.push_back(w);
         }

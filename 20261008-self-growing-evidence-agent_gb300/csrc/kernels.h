@@ -144,6 +144,7 @@ struct WMineParams {
     uint32_t *task_cnt = nullptr;
     int32_t *task_status = nullptr;
     uint64_t *task_nodes = nullptr;
+    uint64_t *task_ns = nullptr;        // optional: device-clock duration of each task
 };
 // Cross-subtree maximality filter of split windows: window wi's tasks, in
 // depth-first subtree order, are entries win_task0[wi] .. win_task0[wi+1]-1

@@ -153,6 +153,12 @@ static_assert(offsetof(WRoot<2>, cand) == 16 && offsetof(WRoot<2>, cand_sup) == 
                   offsetof(WRoot<2>, overflow) == 44 && offsetof(WRoot<2>, f) == 48 && offsetof(WRoot<2>, c) == 176,
               "root record layout read by sgfim_ring_mine_windows");
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // The search stack holds itemsets of up to kWDepth - 1 items.
 constexpr int kWDepth = 48;
 // chunks of 32 entries loaded before any is processed (memory-level parallelism)
@@ -460,6 +466,7 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
         if (lane == 0) ti = atomicAdd(p.next, 1u);
         ti = __shfl_sync(kFull, ti, 0);
         if (ti >= p.n_tasks) break;
+        const uint64_t t_begin = globaltimer_ns();
         const uint32_t t = p.task_order[ti];
         const uint32_t w = p.task_win[t];
         const uint32_t child = p.task_child[t];
@@ -684,6 +691,7 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
             p.task_cnt[t] = status == 0 ? np : 0;
             p.task_status[t] = status;
             p.task_nodes[t] = nodes;
+            if (p.task_ns) p.task_ns[t] = globaltimer_ns() - t_begin;
         }
         __syncwarp();
     }

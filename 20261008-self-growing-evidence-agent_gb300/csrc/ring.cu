@@ -345,12 +345,15 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
     uint8_t *d_keep = nullptr;
     std::vector<uint64_t> t_win_of;          // task -> window
     std::vector<uint32_t> kept;              // per task: candidates kept
+    uint32_t task_warps = 0;
+    double task_kernel_ms = 0.0, task_ms_max = 0.0, task_ms_sum = 0.0;
     try {
         SG_CUDA_TRY(cudaSetDevice(h->device));
         cudaStream_t st = h->stream;
         if (r->hm.ptr && n_windows) {
-            // windows of at least kSplitMin transactions are split at the root
-            constexpr uint64_t kSplitMin = 4096;
+            // windows of at least kSplitMin transactions are split at the root: even a short
+            // window's tree has tens of thousands of nodes, too many for one warp in a batch
+            constexpr uint64_t kSplitMin = 64;
             uint64_t max_len = 0;
             std::vector<uint32_t> split;
             for (uint64_t w = 0; w < n_windows; ++w) {
@@ -454,6 +457,8 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 kernel_ms += timed_ms();
             }
             auto root_at = [&](uint64_t w) { return roots_h.data() + (size_t)w * root_b; };
+            // cost estimate of a subtree: its database size plus a fixed per-node share, per tail item
+            auto child_cost = [](uint32_t sup, uint32_t tail) { return ((double)sup + 512.0) * (double)tail; };
             std::vector<uint8_t> is_split(n_windows, 0), bad(n_windows, 0);
             for (uint32_t w : split) is_split[w] = 1;
             // ---- 2. the costliest root children are split again (their own expansion in wsub_kernel)
@@ -465,7 +470,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 }
                 const unsigned char *R = root_at(w);
                 const uint32_t k = u32_at(R, o_has) ? 0 : u32_at(R, o_k);
-                for (uint32_t j = 0; j < k; ++j) total_cost += (double)u32_at(R, o_c + 4 * j) * (double)(k - j);
+                for (uint32_t j = 0; j < k; ++j) total_cost += child_cost(u32_at(R, o_c + 4 * j), k - j);
             }
             const double split_above = total_cost / (double)(warps * 2);
             std::vector<uint32_t> sub_win, sub_child;
@@ -476,7 +481,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 if (u32_at(R, o_has)) continue;
                 const uint32_t k = u32_at(R, o_k);
                 for (uint32_t j = 0; j + 2 < k; ++j)
-                    if ((double)u32_at(R, o_c + 4 * j) * (double)(k - j) > split_above) {
+                    if (child_cost(u32_at(R, o_c + 4 * j), k - j) > split_above) {
                         sub_win.push_back(w);
                         sub_child.push_back(j);
                     }
@@ -540,12 +545,11 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                         } else {
                             const uint32_t k1 = u32_at(S, o_k);
                             for (uint32_t g = 0; g < k1; ++g)
-                                add_task((uint32_t)w, j, si, g, (double)u32_at(S, o_c + 4 * g) * (double)(k1 - g));
+                                add_task((uint32_t)w, j, si, g, child_cost(u32_at(S, o_c + 4 * g), k1 - g));
                         }
                         ++si;
                     } else {
-                        add_task((uint32_t)w, j, kWholeWindow, kWholeWindow,
-                                 (double)u32_at(R, o_c + 4 * j) * (double)(k - j));
+                        add_task((uint32_t)w, j, kWholeWindow, kWholeWindow, child_cost(u32_at(R, o_c + 4 * j), k - j));
                     }
                 }
             }
@@ -558,7 +562,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             // task arrays: win | child | sub | gchild | order | cnt | kept | status (u32) | off | nodes (u64)
             const size_t nt1 = std::max<uint64_t>(nt, 1);
             const size_t u32_bytes = (8 * 4 * nt1 + 15) & ~(size_t)15;
-            ws.tasks.reserve(u32_bytes + 2 * 8 * nt1, st);
+            ws.tasks.reserve(u32_bytes + 3 * 8 * nt1, st);
             uint32_t *dt_win = ws.tasks.as<uint32_t>();
             uint32_t *dt_child = dt_win + nt1;
             uint32_t *dt_sub = dt_child + nt1;
@@ -569,6 +573,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             int32_t *dt_status = reinterpret_cast<int32_t *>(dt_kept + nt1);
             uint64_t *dt_off = reinterpret_cast<uint64_t *>(ws.tasks.as<char>() + u32_bytes);
             uint64_t *dt_nodes = dt_off + nt1;
+            uint64_t *dt_ns = dt_nodes + nt1;
             d_task_off = dt_off;
             d_task_cnt = dt_cnt;
             if (nt) {
@@ -590,6 +595,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 p.task_cnt = dt_cnt;
                 p.task_status = dt_status;
                 p.task_nodes = dt_nodes;
+                p.task_ns = dt_ns;
                 // ---- 4. all tasks in one persistent launch
                 const uint64_t use_warps = std::min<uint64_t>(warps, (nt + 3) & ~3ull);
                 SG_CUDA_TRY(cudaEventRecord(k0, st));
@@ -598,14 +604,21 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 ++launches;
                 ++h->launches;
                 std::vector<uint32_t> cnt_h(nt), st_h(nt);
-                std::vector<uint64_t> nodes_h(nt);
+                std::vector<uint64_t> nodes_h(nt), ns_h(nt);
+                SG_CUDA_TRY(cudaMemcpyAsync(ns_h.data(), dt_ns, nt * 8, cudaMemcpyDeviceToHost, st));
                 SG_CUDA_TRY(cudaMemcpyAsync(cnt_h.data(), dt_cnt, nt * 4, cudaMemcpyDeviceToHost, st));
                 SG_CUDA_TRY(cudaMemcpyAsync(st_h.data(), dt_status, nt * 4, cudaMemcpyDeviceToHost, st));
                 SG_CUDA_TRY(cudaMemcpyAsync(nodes_h.data(), dt_nodes, nt * 8, cudaMemcpyDeviceToHost, st));
                 uint64_t used = 0;
                 SG_CUDA_TRY(cudaMemcpyAsync(&used, p.out_pos, 8, cudaMemcpyDeviceToHost, st));
                 h->sync();
-                kernel_ms += timed_ms();
+                task_kernel_ms = timed_ms();
+                kernel_ms += task_kernel_ms;
+                task_warps = (uint32_t)use_warps;
+                for (uint64_t t = 0; t < nt; ++t) {
+                    task_ms_max = std::max(task_ms_max, ns_h[t] * 1e-6);
+                    task_ms_sum += ns_h[t] * 1e-6;
+                }
                 used = std::min<uint64_t>(used, out_cap);
                 for (uint64_t t = 0; t < nt; ++t) {
                     nodes[t_win[t]] += nodes_h[t];
@@ -849,6 +862,11 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
     R->elapsed_s = std::chrono::duration<double>(clk::now() - t0).count();
     R->kernel_ms = kernel_ms;
     R->launches = launches;
+    R->warps = task_warps;
+    R->tasks = n_tasks_total;
+    R->task_kernel_ms = task_kernel_ms;
+    R->task_ms_max = task_ms_max;
+    R->task_ms_sum = task_ms_sum;
     *out = R;
     return SGFIM_OK;
 }

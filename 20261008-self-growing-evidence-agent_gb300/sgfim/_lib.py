@@ -75,7 +75,8 @@ class WindowsResult(C.Structure):
     _fields_ = [("n_windows", C.c_uint64), ("mask_words", C.c_uint32), ("offset", u64p), ("masks", u64p),
                 ("support", u32p), ("status", C.POINTER(C.c_int32)), ("nodes", u64p),
                 ("batched", C.POINTER(C.c_uint8)), ("elapsed_s", C.c_double), ("kernel_ms", C.c_double),
-                ("launches", C.c_uint32)]
+                ("launches", C.c_uint32), ("warps", C.c_uint32), ("tasks", C.c_uint64),
+                ("task_kernel_ms", C.c_double), ("task_ms_max", C.c_double), ("task_ms_sum", C.c_double)]
 
 
 class TfMeta(C.Structure):

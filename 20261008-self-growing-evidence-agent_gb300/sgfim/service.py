@@ -120,6 +120,11 @@ class WindowsMined:
         self.elapsed_s = float(r.elapsed_s)
         self.kernel_ms = float(r.kernel_ms)
         self.launches = int(r.launches)
+        self.warps = int(r.warps)
+        self.tasks = int(r.tasks)
+        self.task_kernel_ms = float(r.task_kernel_ms)
+        self.task_ms_max = float(r.task_ms_max)
+        self.task_ms_sum = float(r.task_ms_sum)
 
     def __len__(self):
         return len(self.status)

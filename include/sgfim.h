@@ -347,6 +347,11 @@ typedef struct sgfim_windows_result {
     double elapsed_s;      /* whole call */
     double kernel_ms;      /* batched kernel(s), device time */
     uint32_t launches;     /* batched kernel launches */
+    uint32_t warps;        /* warps of the task launch */
+    uint64_t tasks;        /* search tasks (whole windows and root subtrees) */
+    double task_kernel_ms; /* device time of the task launch */
+    double task_ms_max;    /* longest single task (device clock) */
+    double task_ms_sum;    /* all tasks' device time; / warps = mean busy time of a warp */
 } sgfim_windows_result;
 int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *starts, const uint64_t *lens,
                             const uint32_t *min_counts, uint64_t n_windows, sgfim_windows_result **out);

@@ -116,10 +116,11 @@ struct Staged {
 // handle across calls: per-warp workspaces, the output arena, the window
 // table and its per-window results.
 struct WindowWorkspace {
-    DevBuf lists, lmfi, pool_m, pool_s, levels, out_m, out_s, ctrl, table, res, sub, tasks;
+    DevBuf lists, lmfi, pool_m, pool_s, levels, out_m, out_s, ctrl, table, res, sub, tasks, vbuf;
     HostBuf h_table, h_res, h_out;
     void release() {
-        for (DevBuf *b : {&lists, &lmfi, &pool_m, &pool_s, &levels, &out_m, &out_s, &ctrl, &table, &res, &sub, &tasks})
+        for (DevBuf *b : {&lists, &lmfi, &pool_m, &pool_s, &levels, &out_m, &out_s, &ctrl, &table, &res, &sub, &tasks,
+                          &vbuf})
             b->release();
         h_table.release();
         h_res.release();

@@ -145,7 +145,12 @@ struct WMineParams {
     int32_t *task_status = nullptr;
     uint64_t *task_nodes = nullptr;
     uint64_t *task_ns = nullptr;        // optional: device-clock duration of each task
+    // vertical search (when set): per warp (128 + wmine_depth()) x v_words u32 -- 128 item rows over
+    // the task database's entries, then one tidset per search level
+    uint32_t *vbuf = nullptr;
+    uint32_t v_words = 0;
 };
+int wmine_depth();
 // Cross-subtree maximality filter of split windows: window wi's tasks, in
 // depth-first subtree order, are entries win_task0[wi] .. win_task0[wi+1]-1
 // of task_of[]; task_first[entry] is the window-relative index of the task's

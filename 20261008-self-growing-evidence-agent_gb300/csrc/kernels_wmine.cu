@@ -310,6 +310,88 @@ __device__ __forceinline__ uint32_t build_child(bool ring, const WMineParams &p,
     return dst + cn > p.list_cap ? 0xffffffffu : cn;
 }
 
+
+// Position of item e among the items of T0: its row slot in the vertical layout.
+template <int MW> __device__ __forceinline__ uint32_t m_rank(const Mask<MW> &T0, uint32_t e) {
+    uint32_t r = 0;
+    const uint32_t wi = e >> 6;
+#pragma unroll
+    for (int k = 0; k < MW; ++k) {
+        const uint64_t below = (uint32_t)k < wi ? ~0ull : ((uint32_t)k == wi ? ((1ull << (e & 63)) - 1) : 0ull);
+        r += __popcll(T0.w[k] & below);
+    }
+    return r;
+}
+
+// Vertical rows of a database of n0 entries: bit i of word c of row slot s is
+// set when entry 32c+i holds the s-th item of T0 (entries are restricted to T0).
+template <int MW>
+__device__ __forceinline__ void build_rows(const uint64_t *lists, uint32_t n0, const Mask<MW> &T0, uint32_t *rows,
+                                           uint32_t vw, uint32_t lane) {
+    const uint32_t W = (n0 + 31) / 32;
+    for (uint32_t c = 0; c < W; ++c) {
+        const uint32_t i = c * 32 + lane;
+        const Mask<MW> m = i < n0 ? m_load<MW>(lists + (uint64_t)i * MW) : m_zero<MW>();
+        uint32_t mine = 0, slot = 0;
+#pragma unroll
+        for (int ww = 0; ww < MW; ++ww) {
+            const uint64_t mw_ = m.w[ww];
+            uint64_t x = T0.w[ww];
+            while (x) {
+                const uint32_t bit = __ffsll((long long)x) - 1;
+                x &= x - 1;
+                const uint32_t word = __ballot_sync(kFull, (mw_ >> bit) & 1ull);
+                if (lane == (slot & 31)) mine = word;
+                ++slot;
+                if ((slot & 31) == 0) rows[(uint64_t)(slot - 32 + lane) * vw + c] = mine;
+            }
+        }
+        if ((slot & 31) && lane < (slot & 31)) rows[(uint64_t)((slot & ~31u) + lane) * vw + c] = mine;
+    }
+    __syncwarp();
+}
+
+// c_e = popc(tid AND row(e)) for e in T (lane 0 writes cnt[e]).
+template <int MW>
+__device__ __forceinline__ void vcount(const uint32_t *tid, const uint32_t *rows, uint32_t vw, uint32_t W,
+                                       const Mask<MW> &T, const Mask<MW> &T0, uint32_t *cnt, uint32_t lane) {
+#pragma unroll
+    for (int ww = 0; ww < MW; ++ww) {
+        uint64_t x = T.w[ww];
+        while (x) {
+            const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+            x &= x - 1;
+            const uint32_t *row = rows + (uint64_t)m_rank(T0, e) * vw;
+            uint32_t acc = 0;
+            for (uint32_t w = lane; w < W; w += 32) acc += __popc(tid[w] & row[w]);
+            acc = __reduce_add_sync(kFull, acc);
+            if (lane == 0) cnt[e] = acc;
+        }
+    }
+    __syncwarp();
+}
+
+// |{entries of tid holding every item of F}|
+template <int MW>
+__device__ __forceinline__ uint32_t vcount_superset(const uint32_t *tid, const uint32_t *rows, uint32_t vw, uint32_t W,
+                                                    const Mask<MW> &F, const Mask<MW> &T0, uint32_t lane) {
+    uint32_t acc = 0;
+    for (uint32_t w = lane; w < W; w += 32) {
+        uint32_t v = tid[w];
+#pragma unroll
+        for (int ww = 0; ww < MW; ++ww) {
+            uint64_t x = F.w[ww];
+            while (x && v) {
+                const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+                x &= x - 1;
+                v &= rows[(uint64_t)m_rank(T0, e) * vw + w];
+            }
+        }
+        acc += __popc(v);
+    }
+    return __reduce_add_sync(kFull, acc);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ roots
@@ -697,6 +779,266 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
     }
 }
 
+template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMineParams p) {
+    __shared__ uint32_t s_cnt[4][128];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint64_t warp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    uint32_t *cnt = s_cnt[wib];
+    uint64_t *lists = p.lists + warp * (uint64_t)p.list_cap * MW;
+    uint32_t *lmfi = p.lmfi + warp * (uint64_t)p.lmfi_cap;
+    uint64_t *pool = p.pool_m + warp * (uint64_t)p.pool_cap * MW;
+    uint32_t *pool_s = p.pool_s + warp * (uint64_t)p.pool_cap;
+    WLevel<MW> *LV = reinterpret_cast<WLevel<MW> *>(p.levels) + warp * kWDepth;
+    const WRoot<MW> *roots = reinterpret_cast<const WRoot<MW> *>(p.roots);
+    const uint32_t d = p.d;
+    const uint32_t vw = p.v_words;
+    uint32_t *vrows = p.vbuf + warp * (uint64_t)(128 + kWDepth) * vw;   // row slot s: vrows + s * vw
+    uint32_t *vtid = vrows + (uint64_t)128 * vw;                        // level l: vtid + l * vw
+
+    for (;;) {
+        uint32_t ti = 0;
+        if (lane == 0) ti = atomicAdd(p.next, 1u);
+        ti = __shfl_sync(kFull, ti, 0);
+        if (ti >= p.n_tasks) break;
+        const uint64_t t_begin = globaltimer_ns();
+        const uint32_t t = p.task_order[ti];
+        const uint32_t w = p.task_win[t];
+        const uint32_t child = p.task_child[t];
+        const uint32_t sub = p.task_sub ? p.task_sub[t] : kWholeWindow;
+        const uint32_t gchild = p.task_gchild ? p.task_gchild[t] : kWholeWindow;
+        const uint64_t start = p.starts[w];
+        const uint32_t n = p.lens[w];
+        const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
+        int status = 0;
+        uint32_t np = 0;
+        uint64_t nodes = 0;
+
+        // the task's first node: the whole window, or child `child` of its root
+        bool ring0 = child == kWholeWindow;
+        Mask<MW> H = m_zero<MW>(), T = m_zero<MW>();
+        uint32_t sup = n, list_n = n;
+        bool done = false;   // a split child that is itself terminal: its one candidate
+        if (ring0) {
+            for (uint32_t e = 0; e < d; ++e) m_set(T, e);
+            list_n = build_child<MW>(true, p, start, lists, 0, n, m_zero<MW>(), T, 0, lane);
+            if (list_n == 0xffffffffu) status = 1;
+        } else if (sub == kWholeWindow) {
+            const WRoot<MW> &R = roots[w];
+            const uint32_t k = R.k;
+            for (uint32_t q = child + 1 + lane; q < k; q += 32) m_set(T, R.f[q]);
+            T = warp_or(T);
+            H = m_load<MW>(R.hp);
+            Mask<MW> req = m_zero<MW>();
+            m_set(req, R.f[child]);
+            m_set(H, R.f[child]);
+            sup = R.c[child];
+            list_n = 0;
+            if (m_nz(T)) {
+                list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+                if (list_n == 0xffffffffu) status = 1;
+            }
+        } else {
+            const WRoot<MW> &S = reinterpret_cast<const WRoot<MW> *>(p.subs)[sub];
+            if (S.overflow) {
+                status = 1;
+            } else if (gchild == kWholeWindow) {
+                if (lane < MW) pool[lane] = S.cand[lane];
+                if (lane == 0) pool_s[0] = S.cand_sup;
+                np = 1;
+                nodes = 1;
+                done = true;
+            } else {
+                const uint32_t k1 = S.k;
+                for (uint32_t q = gchild + 1 + lane; q < k1; q += 32) m_set(T, S.f[q]);
+                T = warp_or(T);
+                H = m_load<MW>(S.hp);
+                Mask<MW> req = m_zero<MW>();
+                m_set(req, roots[w].f[child]);
+                m_set(req, S.f[gchild]);
+                m_set(H, S.f[gchild]);
+                sup = S.c[gchild];
+                list_n = 0;
+                if (m_nz(T)) {
+                    list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+                    if (list_n == 0xffffffffu) status = 1;
+                }
+            }
+        }
+        // ---- the task's database as vertical rows over its entries (one row per item of T0)
+        const Mask<MW> T0 = T;
+        const uint32_t W = (list_n + 31) / 32;
+        if (status == 0 && !done) {
+            if (W > vw) {
+                status = 1;
+            } else {
+                build_rows<MW>(lists, list_n, T0, vrows, vw, lane);
+                for (uint32_t x = lane; x < W; x += 32)
+                    vtid[x] = (x + 1 < W || (list_n & 31) == 0) ? 0xffffffffu : ((1u << (list_n & 31)) - 1);
+                __syncwarp();
+            }
+        }
+        int l = 0;
+        uint32_t lm_off = 0, lm_n = 0, entry = 0;
+        bool expand = true;
+
+        while (status == 0 && !done) {
+            if (expand) {
+                expand = false;
+                ++nodes;
+                const uint32_t *tid = vtid + (uint64_t)l * vw;
+                vcount<MW>(tid, vrows, vw, W, T, T0, cnt, lane);
+                Mask<MW> P, F;
+                classify<MW>(T, cnt, d, thr, sup, lane, P, F);
+                Mask<MW> Hp, Q;
+                uint32_t k = 0;
+#pragma unroll
+                for (int i = 0; i < MW; ++i) {
+                    Hp.w[i] = H.w[i] | P.w[i];
+                    Q.w[i] = Hp.w[i] | F.w[i];
+                    k += __popcll(F.w[i]);
+                }
+                // ---- is H u P u F inside a known MFI?  (local list; nothing was found since entry)
+                bool hit = false;
+                for (uint32_t b = 0; b < lm_n && !hit; b += 32 * kU) {
+                    uint32_t idx[kU];
+#pragma unroll
+                    for (int u = 0; u < kU; ++u) {
+                        const uint32_t i = b + u * 32 + lane;
+                        idx[u] = i < lm_n ? lmfi[lm_off + i] : 0xffffffffu;
+                    }
+                    bool h = false;
+#pragma unroll
+                    for (int u = 0; u < kU; ++u)
+                        if (idx[u] != 0xffffffffu) h |= m_sub(Q, m_load<MW>(pool + (uint64_t)idx[u] * MW));
+                    hit = __any_sync(kFull, h);
+                }
+                if (k == 0 || hit) {
+                    if (k == 0 && !hit && m_nz(Hp)) {
+                        if (np >= p.pool_cap) { status = 1; break; }
+                        if (lane < MW) pool[(uint64_t)np * MW + lane] = m_word(Hp, lane);
+                        if (lane == 0) pool_s[np] = sup;
+                        ++np;
+                    }
+                    if (l == 0) break;
+                    --l;
+                    __syncwarp();
+                    continue;
+                }
+                // ---- FHUT: support of H u P u F
+                const uint32_t cf = vcount_superset<MW>(tid, vrows, vw, W, F, T0, lane);
+                if (cf >= thr) {
+                    if (np >= p.pool_cap) { status = 1; break; }
+                    if (lane < MW) pool[(uint64_t)np * MW + lane] = m_word(Q, lane);
+                    if (lane == 0) pool_s[np] = cf;
+                    ++np;
+                    if (l == 0) break;
+                    --l;
+                    __syncwarp();
+                    continue;
+                }
+                // ---- record the node: frequent tail sorted by (support, id)
+                WLevel<MW> &A = LV[l];
+                sort_tail<MW>(F, cnt, lane, A.f, A.c);
+                if (lane < MW) A.hp[lane] = m_word(Hp, lane);
+                if (lane == 0) {
+                    A.lm_off = lm_off;
+                    A.lm_n = lm_n;
+                    A.entry = entry;
+                    A.k = k;
+                    A.j = 0;
+                }
+                __syncwarp();
+            }
+            // ---- next child of level l, or up
+            WLevel<MW> &A = LV[l];
+            const uint32_t j = A.j, k = A.k;
+            if (j >= k) {
+                if (l == 0) break;
+                --l;
+                continue;
+            }
+            __syncwarp();
+            if (lane == 0) A.j = j + 1;
+            const uint32_t e = A.f[j];
+            const uint32_t csup = A.c[j];
+            Mask<MW> Tc = m_zero<MW>();
+            for (uint32_t q = j + 1 + lane; q < k; q += 32) m_set(Tc, A.f[q]);
+            Tc = warp_or(Tc);
+            Mask<MW> Hc = m_load<MW>(A.hp);
+            m_set(Hc, e);
+            {
+                // child tidset = parent tidset AND row(e)
+                const uint32_t *ptid = vtid + (uint64_t)l * vw;
+                uint32_t *ctid = vtid + (uint64_t)(l + 1) * vw;
+                const uint32_t *row = vrows + (uint64_t)m_rank(T0, e) * vw;
+                if (l + 1 < kWDepth)
+                    for (uint32_t x = lane; x < W; x += 32) ctid[x] = ptid[x] & row[x];
+            }
+            // child local-MFI list: members containing the child's head
+            const uint32_t c_lm = A.lm_off + A.lm_n;
+            const uint32_t p_lm_off = A.lm_off, p_lm_n = A.lm_n, p_entry = A.entry;
+            const uint32_t n_src = p_lm_n + (np - p_entry);
+            uint32_t ln = 0;
+            for (uint32_t b = 0; b < n_src; b += 32 * kU) {
+                uint32_t idx[kU];
+                bool keep[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const uint32_t i = b + u * 32 + lane;
+                    idx[u] = 0;
+                    keep[u] = false;
+                    if (i < n_src) idx[u] = i < p_lm_n ? lmfi[p_lm_off + i] : p_entry + (i - p_lm_n);
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u)
+                    if (b + u * 32 + lane < n_src) keep[u] = m_sub(Hc, m_load<MW>(pool + (uint64_t)idx[u] * MW));
+                // the child's list goes after the parent's: writes never touch indices still to be read
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const uint32_t bal = __ballot_sync(kFull, keep[u]);
+                    const uint64_t pos = (uint64_t)c_lm + ln + __popc(bal & ((1u << lane) - 1));
+                    if (keep[u] && pos < p.lmfi_cap) lmfi[pos] = idx[u];
+                    ln += __popc(bal);
+                }
+            }
+            if ((uint64_t)c_lm + ln > p.lmfi_cap) { status = 1; break; }
+            if (l + 1 >= kWDepth) { status = 1; break; }
+            __syncwarp();
+            ++l;
+            H = Hc;
+            T = Tc;
+            sup = csup;
+            lm_off = c_lm;
+            lm_n = ln;
+            entry = np;
+            expand = true;
+        }
+
+        // ---- publish the task's candidates
+        uint64_t off = 0;
+        if (status == 0) {
+            if (lane == 0) off = atomicAdd(p.out_pos, (unsigned long long)np);
+            off = __shfl_sync(kFull, off, 0);
+            if (off + np > p.out_cap) {
+                status = 2;
+            } else {
+                __syncwarp();
+                for (uint32_t i = lane; i < np * MW; i += 32) p.out_m[off * MW + i] = pool[i];
+                for (uint32_t i = lane; i < np; i += 32) p.out_s[off + i] = pool_s[i];
+            }
+        }
+        if (lane == 0) {
+            p.task_off[t] = off;
+            p.task_cnt[t] = status == 0 ? np : 0;
+            p.task_status[t] = status;
+            p.task_nodes[t] = nodes;
+            if (p.task_ns) p.task_ns[t] = globaltimer_ns() - t_begin;
+        }
+        __syncwarp();
+    }
+}
+
 // ------------------------------------------------------------------ cross-task filter
 // One CTA per split window: the window's candidates in task order (subtrees
 // in depth-first order) get a vertical bitmap rows[e][q]; candidate q of a
@@ -804,6 +1146,7 @@ template <int MW> __global__ void __launch_bounds__(128) wgather_kernel(WGatherP
     }
 }
 
+int wmine_depth() { return kWDepth; }
 size_t wmine_level_bytes(int mw) { return mw == 2 ? sizeof(WLevel<2>) * kWDepth : 0; }
 size_t wmine_root_bytes(int mw) { return mw == 2 ? sizeof(WRoot<2>) : 0; }
 
@@ -819,7 +1162,10 @@ void launch_wsub(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st)
 }
 void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st) {
     if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
-    wtask_kernel<2><<<blocks, 128, 0, st>>>(p);
+    if (p.vbuf)
+        wvtask_kernel<2><<<blocks, 128, 0, st>>>(p);
+    else
+        wtask_kernel<2><<<blocks, 128, 0, st>>>(p);
     SG_CUDA_TRY(cudaGetLastError());
 }
 void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st) {

@@ -362,7 +362,11 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             }
             const uint64_t list_cap = std::min<uint64_t>(std::max<uint64_t>(8192, 2 * max_len + 1024), 1ull << 30);
             const uint64_t lmfi_cap = 1u << 16, pool_cap = 1u << 16;
-            const size_t per_warp = list_cap * mw * 8 + lmfi_cap * 4 + pool_cap * (mw * 8 + 4) + wmine_level_bytes(mw);
+            const bool vertical = !(h->flags & SGFIM_F_WINDOWS_HORIZONTAL);
+            const uint64_t v_words = vertical ? (max_len + 31) / 32 + 1 : 0;
+            const size_t v_bytes = (size_t)(128 + wmine_depth()) * v_words * 4;
+            const size_t per_warp =
+                list_cap * mw * 8 + lmfi_cap * 4 + pool_cap * (mw * 8 + 4) + wmine_level_bytes(mw) + v_bytes;
             uint64_t warps = (uint64_t)h->n_sm * 24;
             warps = std::min<uint64_t>(warps, std::max<uint64_t>(4, (h->hbm_budget / 2) / per_warp));
             warps = std::max<uint64_t>(4, warps & ~3ull);
@@ -375,6 +379,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             ws.pool_m.reserve(warps * pool_cap * mw * 8, st);
             ws.pool_s.reserve(warps * pool_cap * 4, st);
             ws.levels.reserve(warps * wmine_level_bytes(mw), st);
+            if (vertical) ws.vbuf.reserve(warps * v_bytes, st);
             ws.out_m.reserve(out_cap * mw * 8, st);
             ws.out_s.reserve(out_cap * 5, st);   // supports, then the keep flags
             ws.ctrl.reserve(256, st);
@@ -432,6 +437,8 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             p.pool_s = ws.pool_s.as<uint32_t>();
             p.pool_cap = (uint32_t)pool_cap;
             p.levels = ws.levels.ptr;
+            p.vbuf = vertical ? ws.vbuf.as<uint32_t>() : nullptr;
+            p.v_words = (uint32_t)v_words;
             p.out_m = ws.out_m.as<uint64_t>();
             p.out_s = ws.out_s.as<uint32_t>();
             p.out_cap = out_cap;

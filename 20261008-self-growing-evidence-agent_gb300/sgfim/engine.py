@@ -81,10 +81,11 @@ class MineResult:
 
 class Engine:
     def __init__(self, device=0, hbm_budget=0, wave_nodes=0, verbose=False, phase_timers=False,
-                 ignore_id0=False, blocking_sync=False):
+                 ignore_id0=False, blocking_sync=False, windows_horizontal=False):
         self._L = L.load()
         flags = (L.F_VERBOSE if verbose else 0) | (L.F_PHASE_TIMERS if phase_timers else 0) | \
-            (L.F_IGNORE_ID0 if ignore_id0 else 0) | (L.F_BLOCKING_SYNC if blocking_sync else 0)
+            (L.F_IGNORE_ID0 if ignore_id0 else 0) | (L.F_BLOCKING_SYNC if blocking_sync else 0) | \
+            (L.F_WINDOWS_HORIZONTAL if windows_horizontal else 0)
         cfg = L.Config(device, hbm_budget, wave_nodes, flags, None)
         h = C.c_void_p()
         rc = self._L.sgfim_open(C.byref(cfg), C.byref(h))

@@ -66,6 +66,9 @@ typedef struct {
 #define SGFIM_F_PHASE_TIMERS 0x4u /* record per-kernel CUDA events in support-batch calls */
 #define SGFIM_F_BLOCKING_SYNC 0x8u /* the miner waits for the device by sleeping, not spinning
                                       (many concurrent handles on few host cores) */
+#define SGFIM_F_WINDOWS_HORIZONTAL 0x10u /* sgfim_ring_mine_windows searches each task on horizontal
+                                            item masks instead of vertical rows (slower; kept for
+                                            comparison) */
 
 /* Open a handle on a device.  Replaces the engines' process start-up
  * (kernel_bitmap.cu:796-800, AnytimeMining/kernel.cu:798-805). */

@@ -74,15 +74,18 @@ def test_service_windows_exact(mode):
         assert rq.result.as_dict() == _oracle_mfis(rows[rq.end - length:rq.end], thr), rq.idx
 
 
-def test_ring_mine_windows_batched(engine):
+@pytest.mark.parametrize("horizontal", [False, True], ids=["vertical", "horizontal"])
+def test_ring_mine_windows_batched(horizontal):
     """One batched launch over windows of every size class, including the
     empty window, floors above the window length and floor 1, with the ring
     wrapped: each window's MFIs equal the oracle's, and the kernel (not the
     wave miner) mined them."""
+    from sgfim.engine import Engine
     from sgfim.service import Ring
     rows = datagen.regime_txns(300_000, 21, 6, 8, 0.3, seed=11)
     rp, it = datagen.txns_to_csr(rows)
     ring = Ring(126, 1 << 17)
+    engine = Engine(windows_horizontal=horizontal)
     try:
         ring.append(rp, it)            # wraps: the ring keeps the newest 131,072
         head = ring.head
@@ -116,6 +119,7 @@ def test_ring_mine_windows_batched(engine):
             ring.mine_windows(engine, [0], [10], [1])
     finally:
         ring.close()
+        engine.close()
 
 
 def test_appends_wait_for_windows_being_mined(engine):

@@ -109,6 +109,8 @@ constexpr uint32_t kWholeWindow = 0xffffffffu;
 struct WMineParams {
     const uint64_t *hm = nullptr;   // ring horizontal masks [capacity][MW]
     uint64_t cap_mask = 0;          // ring capacity (transactions, power of two) - 1
+    const uint64_t *ring_rows = nullptr;  // ring vertical rows [d][ring_words]
+    uint64_t ring_words = 0;              // capacity / 64
     uint32_t d = 0;
     const uint64_t *starts = nullptr;   // per window
     const uint32_t *lens = nullptr;

@@ -395,12 +395,16 @@ __device__ __forceinline__ uint32_t vcount_superset(const uint32_t *tid, const u
 }  // namespace
 
 // ------------------------------------------------------------------ roots
+// Root counts from the ring's vertical rows: item e's support in the window
+// is the popcount of its row over the window's bit range (the ring keeps
+// one row per item, 64 transactions per word).
 template <int MW> __global__ void __launch_bounds__(128) wroot_kernel(WMineParams p) {
     __shared__ uint32_t s_cnt[4][128];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;
     uint32_t *cnt = s_cnt[wib];
     WRoot<MW> *roots = reinterpret_cast<WRoot<MW> *>(p.roots);
+    const uint64_t cwm = p.ring_words - 1;   // ring words: a power of two
     for (;;) {
         uint32_t wi = 0;
         if (lane == 0) wi = atomicAdd(p.next + 1, 1u);
@@ -410,9 +414,27 @@ template <int MW> __global__ void __launch_bounds__(128) wroot_kernel(WMineParam
         const uint64_t start = p.starts[w];
         const uint32_t n = p.lens[w];
         const uint32_t thr = p.thrs[w] ? p.thrs[w] : 1;
+        // window bits: unwrapped words w0 .. w1, masked at both ends
+        const uint64_t w0 = start >> 6, w1 = n ? (start + n - 1) >> 6 : w0;
+        const uint64_t nwd = n ? w1 - w0 + 1 : 0;
+        const uint64_t m_first = ~0ull << (start & 63);
+        const uint64_t m_last = n ? (~0ull >> (63 - ((start + n - 1) & 63))) : 0;
+        auto word_mask = [&](uint64_t i) {
+            uint64_t m = ~0ull;
+            if (i == 0) m &= m_first;
+            if (i + 1 == nwd) m &= m_last;
+            return m;
+        };
         Mask<MW> T = m_zero<MW>();
         for (uint32_t e = 0; e < p.d; ++e) m_set(T, e);
-        count_items<MW>(true, p, start, nullptr, 0, n, T, cnt, lane);
+        for (uint32_t e = 0; e < p.d; ++e) {
+            const uint64_t *row = p.ring_rows + (uint64_t)e * p.ring_words;
+            uint32_t acc = 0;
+            for (uint64_t i = lane; i < nwd; i += 32) acc += __popcll(row[(w0 + i) & cwm] & word_mask(i));
+            acc = __reduce_add_sync(kFull, acc);
+            if (lane == 0) cnt[e] = acc;
+        }
+        __syncwarp();
         Mask<MW> P, F;
         classify<MW>(T, cnt, p.d, thr, n, lane, P, F);
         uint32_t k = 0;
@@ -425,7 +447,22 @@ template <int MW> __global__ void __launch_bounds__(128) wroot_kernel(WMineParam
             has = m_nz(P) ? 1u : 0u;
             csup = n;
         } else {
-            const uint32_t cf = count_superset<MW>(true, p, start, nullptr, 0, n, F, lane);
+            // FHUT: transactions holding every item of F
+            uint32_t acc = 0;
+            for (uint64_t i = lane; i < nwd; i += 32) {
+                uint64_t v = word_mask(i);
+#pragma unroll
+                for (int ww = 0; ww < MW; ++ww) {
+                    uint64_t x = F.w[ww];
+                    while (x && v) {
+                        const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+                        x &= x - 1;
+                        v &= p.ring_rows[(uint64_t)e * p.ring_words + ((w0 + i) & cwm)];
+                    }
+                }
+                acc += __popcll(v);
+            }
+            const uint32_t cf = __reduce_add_sync(kFull, acc);
             if (cf >= thr) {
                 has = 1;
                 csup = cf;

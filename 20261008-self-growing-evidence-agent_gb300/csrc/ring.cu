@@ -420,6 +420,8 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             WMineParams p;
             p.hm = r->hm.as<uint64_t>();
             p.cap_mask = cap_bits - 1;
+            p.ring_rows = r->rows.as<uint64_t>();
+            p.ring_words = r->cap_words;
             p.d = r->d;
             p.starts = d_start;
             p.lens = d_len;

@@ -80,10 +80,7 @@ class Ring:
                                              lens.ctypes.data_as(L.u64p), mc.ctypes.data_as(L.u32p), n,
                                              C.byref(res))
         eng._check(rc)
-        try:
-            return WindowsMined(res)
-        finally:
-            self._L.sgfim_windows_result_free(res)
+        return WindowsMined(res, self._L)
 
     def close(self):
         if getattr(self, "_r", None):
@@ -103,17 +100,20 @@ def masks_to_sets(masks):
 
 
 class WindowsMined:
-    """Per-window MFIs of sgfim_ring_mine_windows as numpy arrays."""
+    """Per-window MFIs of sgfim_ring_mine_windows.  The masks and supports are
+    numpy views of the library's result arrays (no copy); the result is freed
+    when this object is."""
 
-    def __init__(self, res_ptr):
+    def __init__(self, res_ptr, lib):
+        self._res, self._L = res_ptr, lib
         r = res_ptr.contents
         n = int(r.n_windows)
         self.mask_words = int(r.mask_words)
         self.offset = np.ctypeslib.as_array(r.offset, shape=(n + 1,)).copy()
         tot = int(self.offset[-1])
-        self.masks = (np.ctypeslib.as_array(r.masks, shape=(tot * self.mask_words,)).reshape(tot, self.mask_words).copy()
+        self.masks = (self._view(r.masks, C.c_uint64, tot * self.mask_words, np.uint64).reshape(tot, self.mask_words)
                       if tot else np.zeros((0, self.mask_words), np.uint64))
-        self.support = np.ctypeslib.as_array(r.support, shape=(tot,)).copy() if tot else np.zeros(0, np.uint32)
+        self.support = self._view(r.support, C.c_uint32, tot, np.uint32) if tot else np.zeros(0, np.uint32)
         self.status = np.ctypeslib.as_array(r.status, shape=(n,)).copy() if n else np.zeros(0, np.int32)
         self.nodes = np.ctypeslib.as_array(r.nodes, shape=(n,)).copy() if n else np.zeros(0, np.uint64)
         self.batched = np.ctypeslib.as_array(r.batched, shape=(n,)).copy() if n else np.zeros(0, np.uint8)
@@ -125,6 +125,17 @@ class WindowsMined:
         self.task_kernel_ms = float(r.task_kernel_ms)
         self.task_ms_max = float(r.task_ms_max)
         self.task_ms_sum = float(r.task_ms_sum)
+
+    def _view(self, ptr, ctype, count, dtype):
+        # the buffer object references this result, so the views keep it (and its memory) alive
+        buf = (ctype * count).from_address(C.addressof(ptr.contents))
+        buf._owner = self
+        return np.frombuffer(buf, dtype=dtype)
+
+    def __del__(self):
+        if getattr(self, "_res", None) is not None:
+            self._L.sgfim_windows_result_free(self._res)
+            self._res = None
 
     def __len__(self):
         return len(self.status)

@@ -421,6 +421,42 @@ def _cpu_window(args):
     return ok, time.perf_counter() - t
 
 
+def saturate(rows, reqs, repeat, horizontal=False, hbm_budget=32 << 30, out=""):
+    """Every request's window (as the service would cut it) in one batched call."""
+    import json
+    rp, it = datagen.txns_to_csr(rows)
+    eng = Engine(hbm_budget=hbm_budget, windows_horizontal=horizontal)
+    ring = Ring(126, WORKLOAD["ring_txn"])
+    try:
+        ring.append(rp, it)
+        total, warm = len(rows), WORKLOAD["len_hi"]
+        ends = np.array([min(total, warm + int(WORKLOAD["stream_rate"] * rq.arrival)) for rq in reqs], np.int64)
+        lens = np.minimum(np.array([rq.length for rq in reqs], np.int64), ends)
+        thrs = np.maximum(1, np.ceil(WORKLOAD["floor_frac"] * lens)).astype(np.int64)
+        reps = []
+        for _ in range(repeat):
+            t = time.perf_counter()
+            res = ring.mine_windows(eng, ends - lens, lens, thrs)
+            dt = time.perf_counter() - t
+            reps.append({"call_s": dt, "kernel_ms": res.kernel_ms, "task_kernel_ms": res.task_kernel_ms,
+                         "task_ms_max": res.task_ms_max, "warps": res.warps, "tasks": res.tasks,
+                         "warp_busy_ms": res.task_ms_sum / max(1, res.warps), "launches": res.launches,
+                         "batched": int(res.batched.sum()), "nodes": int(res.nodes.sum()),
+                         "mfis": int(res.offset[-1]), "windows_per_s": len(reqs) / dt,
+                         "windows_per_s_kernels": len(reqs) / (res.kernel_ms / 1e3)})
+            del res
+        report = {"workload": "windows-4096 (all windows in one call)", "windows": len(reqs),
+                  "mode": "horizontal" if horizontal else "vertical", "runs": reps}
+        print(json.dumps(report))
+        if out:
+            with open(out, "w") as f:
+                json.dump(report, f, indent=1)
+        return report
+    finally:
+        ring.close()
+        eng.close()
+
+
 def main(argv=None):
     import argparse
     import json
@@ -435,9 +471,15 @@ def main(argv=None):
     ap.add_argument("--check-budget-s", type=float, default=240.0)
     ap.add_argument("--cpu-budget-s", type=float, default=30.0)
     ap.add_argument("--out", default="")
+    ap.add_argument("--saturate", type=int, default=0, metavar="REPEAT",
+                    help="instead of the timed service, mine every request's window in one "
+                         "sgfim_ring_mine_windows call, REPEAT times (capacity of the batched miner)")
+    ap.add_argument("--horizontal", action="store_true", help="batched miner on horizontal masks")
     a = ap.parse_args(argv)
     rows = stream_rows_for(a.requests)
     reqs = make_requests(a.requests, WORKLOAD["rate_hz"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
+    if a.saturate:
+        return saturate(rows, reqs, a.saturate, a.horizontal, int(a.hbm_budget_gb * (1 << 30)), a.out)
     svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
                         keep_results=a.check, mode=a.mode)
     # warm-up pass on a handful of requests (first-use allocations of every worker)

@@ -189,7 +189,8 @@ typedef struct {
 int sgfim_phase_stats_get(sgfim_handle *h, sgfim_phase_stats *out, int reset);
 
 /* Device-pointer form: bitmaps as in sgfim_support_batch_device, out d*d
- * uint32 in device memory.  kind: SGFIM_COOC_* (AUTO picks the tuned one). */
+ * uint32 in device memory.  kind: SGFIM_COOC_* (AUTO: the tcgen05 kernel, or the popcount
+ * kernel when the bitmaps are not 16-byte aligned). */
 #define SGFIM_COOC_AUTO 0
 #define SGFIM_COOC_POPC 1     /* CUDA-core AND + popc, register tiled */
 #define SGFIM_COOC_BMMA 2     /* b1 mma.sync AND-POPC on the tensor pipe */

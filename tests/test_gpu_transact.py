@@ -44,3 +44,30 @@ def test_transactionize_rejects_bad_input(engine):
         engine.transactionize(vals, 10, 5, 3)
     with pytest.raises(SgfimError):
         engine.transactionize(np.ones((400, 2)), 300, 5, 3)    # window > 256
+
+
+def test_stream_to_windows_pipeline(engine):
+    """Sensor stream -> transactions on the GPU -> device ring -> batched window
+    mining: every window equals the oracle run on the oracle's own
+    transactionisation of the same stream."""
+    import oracle
+    from sgfim.service import Ring
+    vals, anom = datagen.sensor_stream(60_000, 21, 21, constant_cols=(4,))
+    items, labels, edges = engine.transactionize(vals, 30, 15, 6, anomaly=anom)
+    w_items, _ = transact.window_items(vals, transact.fit_bins(vals, 6), 30, 15, anom, 6)
+    assert np.array_equal(items, w_items)
+    rp, it = datagen.txns_to_csr(items)
+    ring = Ring(126, 1 << 13)
+    try:
+        ring.append(rp, it)
+        n = len(items)
+        starts, lens = [0, 100, n - 3000, n - 500], [n, 2500, 3000, 500]
+        thrs = [max(1, int(np.ceil(0.03 * L))) for L in lens]
+        res = ring.mine_windows(engine, starts, lens, thrs)
+        for w, (s, L, t) in enumerate(zip(starts, lens, thrs)):
+            srp, sit = datagen.txns_to_csr(w_items[s:s + L])
+            bm, _ = oracle.build_bitmaps(srp, sit, 126)
+            ref, _ = oracle.mine_fast(bm, L, t)
+            assert res.as_dict(w) == {frozenset(x): c for x, c in ref}, w
+    finally:
+        ring.close()

@@ -1083,10 +1083,17 @@ template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMinePara
 // first candidate.  keep[] is written per arena slot, kept[] per task.
 template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterParams p) {
     __shared__ uint32_t s_w;
+    __shared__ uint32_t s_freq[64 * MW];              // candidates holding each item
+    __shared__ uint32_t s_lo[64 * MW], s_hi[64 * MW];  // first / last word of each item's row with a bit
     uint64_t *rows = p.scratch + (uint64_t)blockIdx.x * p.scratch_words;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_w = atomicAdd(p.next, 1u);
+        for (uint32_t i = threadIdx.x; i < 64 * MW; i += blockDim.x) {
+            s_freq[i] = 0;
+            s_lo[i] = 0xffffffffu;
+            s_hi[i] = 0;
+        }
         __syncthreads();
         const uint32_t wi = s_w;
         if (wi >= p.n_win) break;
@@ -1121,6 +1128,9 @@ template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterP
                     x &= x - 1;
                     atomicOr(reinterpret_cast<unsigned long long *>(rows + (uint64_t)e * W + (q >> 6)),
                              1ull << (q & 63));
+                    atomicAdd(&s_freq[e], 1u);
+                    atomicMin(&s_lo[e], (uint32_t)(q >> 6));
+                    atomicMax(&s_hi[e], (uint32_t)(q >> 6));
                 }
             }
         }
@@ -1133,11 +1143,23 @@ template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterP
             const uint64_t lim = p.task_first[en];   // candidates of earlier subtrees: [0, lim)
             if (lim) {
                 const Mask<MW> m = m_load<MW>(p.out_m + slot * MW);
-                uint32_t ef = 0;
+                // the candidate's rarest item drives the scan: its row has the fewest bits
+                uint32_t ef = 0, best = 0xffffffffu;
 #pragma unroll
-                for (int ww = MW - 1; ww >= 0; --ww)
-                    if (m.w[ww]) ef = ww * 64 + (__ffsll((long long)m.w[ww]) - 1);
-                for (uint64_t wd = 0; wd * 64 < lim && keep; ++wd) {
+                for (int ww = 0; ww < MW; ++ww) {
+                    uint64_t x = m.w[ww];
+                    while (x) {
+                        const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+                        x &= x - 1;
+                        if (s_freq[e] < best) {
+                            best = s_freq[e];
+                            ef = e;
+                        }
+                    }
+                }
+                const uint64_t wd_end = (lim + 63) / 64;
+                const uint64_t hi = (uint64_t)s_hi[ef] + 1 < wd_end ? (uint64_t)s_hi[ef] + 1 : wd_end;
+                for (uint64_t wd = s_lo[ef]; wd < hi && keep; ++wd) {
                     uint64_t v = rows[(uint64_t)ef * W + wd];
                     if (wd * 64 + 64 > lim) v &= (1ull << (lim - wd * 64)) - 1;
 #pragma unroll

@@ -153,6 +153,8 @@ struct WMineParams {
     uint32_t v_words = 0;
 };
 int wmine_depth();
+// resident 128-thread blocks of the task kernel per SM (registers bound it)
+int wtask_blocks_per_sm(bool vertical);
 // Cross-subtree maximality filter of split windows: window wi's tasks, in
 // depth-first subtree order, are entries win_task0[wi] .. win_task0[wi+1]-1
 // of task_of[]; task_first[entry] is the window-relative index of the task's

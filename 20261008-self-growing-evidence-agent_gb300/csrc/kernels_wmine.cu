@@ -311,6 +311,71 @@ __device__ __forceinline__ uint32_t build_child(bool ring, const WMineParams &p,
 }
 
 
+// Base database of a task, found through the ring's vertical rows: the
+// window's transactions holding every item of req (at most two items; none =
+// every transaction), each as its item mask restricted to T, dropped when
+// empty, in transaction order, written at lists[0 ..).  Returns the count, or
+// 0xffffffff when it does not fit.
+template <int MW>
+__device__ __forceinline__ uint32_t build_base(const WMineParams &p, uint64_t start, uint32_t n, const Mask<MW> &req,
+                                               const Mask<MW> &T, uint64_t *lists, uint32_t lane) {
+    uint32_t r0 = 0xffffffffu, r1 = 0xffffffffu;
+#pragma unroll
+    for (int ww = 0; ww < MW; ++ww) {
+        uint64_t x = req.w[ww];
+        while (x) {
+            const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+            x &= x - 1;
+            if (r0 == 0xffffffffu) r0 = e;
+            else r1 = e;
+        }
+    }
+    const uint64_t cwm = p.ring_words - 1;
+    const uint64_t w0 = start >> 6;
+    const uint64_t nwd = n ? ((start + n - 1) >> 6) - w0 + 1 : 0;
+    const uint64_t m_first = ~0ull << (start & 63);
+    const uint64_t m_last = n ? (~0ull >> (63 - ((start + n - 1) & 63))) : 0;
+    uint32_t cn = 0;
+    for (uint64_t b = 0; b < nwd; b += 32) {
+        const uint64_t i = b + lane;
+        uint64_t bits = 0;
+        if (i < nwd) {
+            bits = ~0ull;
+            if (i == 0) bits &= m_first;
+            if (i + 1 == nwd) bits &= m_last;
+            const uint64_t wq = (w0 + i) & cwm;
+            if (r0 != 0xffffffffu) bits &= p.ring_rows[(uint64_t)r0 * p.ring_words + wq];
+            if (r1 != 0xffffffffu) bits &= p.ring_rows[(uint64_t)r1 * p.ring_words + wq];
+        }
+        // pass 1: how many of this lane's transactions keep a tail item
+        uint32_t mine = 0;
+        for (uint64_t x = bits; x; x &= x - 1) {
+            const uint64_t pos = ((w0 + i) << 6) + (__ffsll((long long)x) - 1);
+            mine += m_nz(m_and(m_load<MW>(p.hm + (pos & p.cap_mask) * MW), T));
+        }
+        // exclusive prefix over the lanes keeps transaction order
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        uint64_t at = cn + incl - mine;
+        // pass 2: write them
+        for (uint64_t x = bits; x; x &= x - 1) {
+            const uint64_t pos = ((w0 + i) << 6) + (__ffsll((long long)x) - 1);
+            const Mask<MW> m = m_and(m_load<MW>(p.hm + (pos & p.cap_mask) * MW), T);
+            if (m_nz(m)) {
+                if (at < p.list_cap) m_store(lists + at * MW, m);
+                ++at;
+            }
+        }
+        cn += __shfl_sync(kFull, incl, 31);
+    }
+    __syncwarp();
+    return cn > p.list_cap ? 0xffffffffu : cn;
+}
+
 // Position of item e among the items of T0: its row slot in the vertical layout.
 template <int MW> __device__ __forceinline__ uint32_t m_rank(const Mask<MW> &T0, uint32_t e) {
     uint32_t r = 0;
@@ -858,7 +923,7 @@ template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMinePara
         bool done = false;   // a split child that is itself terminal: its one candidate
         if (ring0) {
             for (uint32_t e = 0; e < d; ++e) m_set(T, e);
-            list_n = build_child<MW>(true, p, start, lists, 0, n, m_zero<MW>(), T, 0, lane);
+            list_n = build_base<MW>(p, start, n, m_zero<MW>(), T, lists, lane);
             if (list_n == 0xffffffffu) status = 1;
         } else if (sub == kWholeWindow) {
             const WRoot<MW> &R = roots[w];
@@ -872,7 +937,7 @@ template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMinePara
             sup = R.c[child];
             list_n = 0;
             if (m_nz(T)) {
-                list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+                list_n = build_base<MW>(p, start, n, req, T, lists, lane);
                 if (list_n == 0xffffffffu) status = 1;
             }
         } else {
@@ -897,7 +962,7 @@ template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMinePara
                 sup = S.c[gchild];
                 list_n = 0;
                 if (m_nz(T)) {
-                    list_n = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+                    list_n = build_base<MW>(p, start, n, req, T, lists, lane);
                     if (list_n == 0xffffffffu) status = 1;
                 }
             }
@@ -1206,6 +1271,13 @@ template <int MW> __global__ void __launch_bounds__(128) wgather_kernel(WGatherP
 }
 
 int wmine_depth() { return kWDepth; }
+
+int wtask_blocks_per_sm(bool vertical) {
+    int blocks = 0;
+    if (vertical) SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, wvtask_kernel<2>, 128, 0));
+    else SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, wtask_kernel<2>, 128, 0));
+    return blocks > 0 ? blocks : 1;
+}
 size_t wmine_level_bytes(int mw) { return mw == 2 ? sizeof(WLevel<2>) * kWDepth : 0; }
 size_t wmine_root_bytes(int mw) { return mw == 2 ? sizeof(WRoot<2>) : 0; }
 

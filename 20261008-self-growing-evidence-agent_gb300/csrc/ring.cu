@@ -367,7 +367,7 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             const size_t v_bytes = (size_t)(128 + wmine_depth()) * v_words * 4;
             const size_t per_warp =
                 list_cap * mw * 8 + lmfi_cap * 4 + pool_cap * (mw * 8 + 4) + wmine_level_bytes(mw) + v_bytes;
-            uint64_t warps = (uint64_t)h->n_sm * 24;
+            uint64_t warps = (uint64_t)h->n_sm * 4 * (uint64_t)wtask_blocks_per_sm(vertical);
             warps = std::min<uint64_t>(warps, std::max<uint64_t>(4, (h->hbm_budget / 2) / per_warp));
             warps = std::max<uint64_t>(4, warps & ~3ull);
             const size_t cand_bytes = mw * 8 + 4 + 1;

@@ -420,6 +420,11 @@ __device__ __forceinline__ void build_rows(const uint64_t *lists, uint32_t n0, c
 template <int MW>
 __device__ __forceinline__ void vcount(const uint32_t *tid, const uint32_t *rows, uint32_t vw, uint32_t W,
                                        const Mask<MW> &T, const Mask<MW> &T0, uint32_t *cnt, uint32_t lane) {
+    constexpr uint32_t kReg = 4;   // tidsets of up to 128 words stay in registers across the items
+    uint32_t tr[kReg];
+    const bool small = W <= 32 * kReg;
+#pragma unroll
+    for (uint32_t k = 0; k < kReg; ++k) tr[k] = (small && lane + 32 * k < W) ? tid[lane + 32 * k] : 0u;
 #pragma unroll
     for (int ww = 0; ww < MW; ++ww) {
         uint64_t x = T.w[ww];
@@ -428,7 +433,13 @@ __device__ __forceinline__ void vcount(const uint32_t *tid, const uint32_t *rows
             x &= x - 1;
             const uint32_t *row = rows + (uint64_t)m_rank(T0, e) * vw;
             uint32_t acc = 0;
-            for (uint32_t w = lane; w < W; w += 32) acc += __popc(tid[w] & row[w]);
+            if (small) {
+#pragma unroll
+                for (uint32_t k = 0; k < kReg; ++k)
+                    if (lane + 32 * k < W) acc += __popc(tr[k] & row[lane + 32 * k]);
+            } else {
+                for (uint32_t w = lane; w < W; w += 32) acc += __popc(tid[w] & row[w]);
+            }
             acc = __reduce_add_sync(kFull, acc);
             if (lane == 0) cnt[e] = acc;
         }
@@ -881,7 +892,7 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
     }
 }
 
-template <int MW> __global__ void __launch_bounds__(128) wvtask_kernel(WMineParams p) {
+template <int MW> __global__ void __launch_bounds__(128, 6) wvtask_kernel(WMineParams p) {
     __shared__ uint32_t s_cnt[4][128];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;

@@ -360,9 +360,12 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                 max_len = std::max(max_len, lens[w]);
                 if (lens[w] >= kSplitMin) split.push_back((uint32_t)w);
             }
-            const uint64_t list_cap = std::min<uint64_t>(std::max<uint64_t>(8192, 2 * max_len + 1024), 1ull << 30);
-            const uint64_t lmfi_cap = 1u << 16, pool_cap = 1u << 16;
+            // the vertical search keeps only the task's base database as entries; the horizontal
+            // one stacks every level's database
             const bool vertical = !(h->flags & SGFIM_F_WINDOWS_HORIZONTAL);
+            const uint64_t list_cap = std::min<uint64_t>(
+                std::max<uint64_t>(8192, (vertical ? 1 : 2) * max_len + 1024), 1ull << 30);
+            const uint64_t lmfi_cap = 1u << 16, pool_cap = 1u << 16;
             const uint64_t v_words = vertical ? (max_len + 31) / 32 + 1 : 0;
             const size_t v_bytes = (size_t)(128 + wmine_depth()) * v_words * 4;
             const size_t per_warp =

@@ -45,6 +45,11 @@ void launch_transpose(const uint64_t *row_ptr, const uint32_t *items, uint64_t n
 void launch_row_popc(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t *counts,
                      cudaStream_t st);
 void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm);
+// Counts of every (node, tail item) of a wave whose nodes hold a mask slot:
+// out[j] = popc(arena[slot[i]] AND rows[items[j]]) for tail_ptr[i] <= j < tail_ptr[i+1].
+void launch_tail_counts(const uint64_t *rows, uint64_t row_stride, uint64_t n_words, const uint64_t *arena,
+                        uint64_t arena_stride, const uint32_t *slot, const uint64_t *tail_ptr, uint32_t n_nodes,
+                        uint64_t n_entries, const uint32_t *items, uint32_t *out, cudaStream_t st, int n_sm);
 
 // Batched candidate supports (config "support-1m" path).  Packs CSR candidates
 // into 16-byte records when every item fits 16 bits and k <= 8, runs the

@@ -177,6 +177,45 @@ __global__ void __launch_bounds__(256) query_kernel(QueryBatch qb) {
     }
 }
 
+// Tail counts of a wave's nodes: entry j of the concatenated tails belongs to
+// node i (tail_ptr[i] <= j < tail_ptr[i+1]); out[j] = popc(mask(slot[i]) AND
+// row(items[j])).  One warp per entry, the node found by binary search, so
+// the host builds one record per node instead of one query per tail item.
+__global__ void __launch_bounds__(256) tail_count_kernel(const uint64_t *__restrict__ rows, uint64_t row_stride,
+                                                        uint64_t n_words, const uint64_t *__restrict__ arena,
+                                                        uint64_t arena_stride, const uint32_t *__restrict__ slot,
+                                                        const uint64_t *__restrict__ tail_ptr, uint32_t n_nodes,
+                                                        const uint32_t *__restrict__ items, uint32_t *__restrict__ out) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t total = tail_ptr[n_nodes];
+    for (uint64_t j = warp; j < total; j += n_warps) {
+        uint32_t lo = 0, hi = n_nodes - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (tail_ptr[mid] <= j) lo = mid;
+            else hi = mid - 1;
+        }
+        const uint64_t *mask = arena + (uint64_t)slot[lo] * arena_stride;
+        const uint64_t *row = rows + (uint64_t)items[j] * row_stride;
+        uint32_t acc = 0;
+        for (uint64_t w = 2 * lane; w < n_words; w += 64) acc += popc4(and4(ld_nc_v4(mask + w), ld_nc_v4(row + w)));
+        acc = warp_sum(acc);
+        if (lane == 0) out[j] = acc;
+    }
+}
+
+void launch_tail_counts(const uint64_t *rows, uint64_t row_stride, uint64_t n_words, const uint64_t *arena,
+                        uint64_t arena_stride, const uint32_t *slot, const uint64_t *tail_ptr, uint32_t n_nodes,
+                        uint64_t n_entries, const uint32_t *items, uint32_t *out, cudaStream_t st, int n_sm) {
+    if (n_nodes == 0 || n_entries == 0) return;
+    const uint64_t blocks = std::min<uint64_t>((n_entries + 7) / 8, (uint64_t)n_sm * 64);
+    tail_count_kernel<<<(unsigned)blocks, 256, 0, st>>>(rows, row_stride, n_words, arena, arena_stride, slot, tail_ptr,
+                                                        n_nodes, items, out);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
 void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm) {
     uint64_t blocks;
     if (qb.n_q_device) {

@@ -75,6 +75,7 @@ class Miner {
           q_items_(w_.q_items), q_slot_(w_.q_slot), c_ptr_(w_.c_ptr), c_items_(w_.c_items), c_ps_(w_.c_ps),
           c_cs_(w_.c_cs), p_ptr_(w_.p_ptr), p_items_(w_.p_items), feat_(w_.feat), w0_(w_.w0), q_out_(w_.q_out),
           score_(w_.score), hq_out_(w_.hq_out), hscore_(w_.hscore) {}
+    // (tail-count staging lives in w_: t_ptr, t_items, t_slot, t_out, ht_out)
 
     int run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out);
 
@@ -128,6 +129,8 @@ class Miner {
     }
     void run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d,
                      int mode, std::vector<uint32_t> &out, const uint64_t *w0 = nullptr);
+    void run_tail_counts(const std::vector<uint64_t> &ptr, const std::vector<uint32_t> &items,
+                         const std::vector<uint32_t> &slots, std::vector<uint32_t> &out);
     void pool_reserve(uint64_t members);
     void emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node);
     void flush_pool(uint64_t from);
@@ -159,6 +162,27 @@ void Miner::run_queries(const QuerySet &qs, const uint64_t *rows, uint64_t strid
     SG_CUDA_TRY(cudaMemcpyAsync(hq_out_.ptr, q_out_.ptr, n * 4, cudaMemcpyDeviceToHost, st));
     h_->sync();
     memcpy(out.data(), hq_out_.ptr, n * 4);
+}
+
+// Counts of the tail items of the wave's nodes that hold a mask: one record
+// per node (its slot and tail range), one result per tail entry.
+void Miner::run_tail_counts(const std::vector<uint64_t> &ptr, const std::vector<uint32_t> &items,
+                            const std::vector<uint32_t> &slots, std::vector<uint32_t> &out) {
+    const size_t n = items.size();
+    out.resize(n);
+    if (n == 0) return;
+    cudaStream_t st = h_->stream;
+    const uint64_t *dptr = w_.t_ptr.put(ptr.data(), ptr.size(), st);
+    const uint32_t *ditems = w_.t_items.put(items.data(), n, st);
+    const uint32_t *dslot = w_.t_slot.put(slots.data(), slots.size(), st);
+    w_.t_out.reserve(n * 4, st);
+    w_.ht_out.reserve(n * 4);
+    launch_tail_counts(ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, arena_.as<uint64_t>(), slot_words_, dslot,
+                       dptr, (uint32_t)slots.size(), n, ditems, w_.t_out.as<uint32_t>(), st, h_->n_sm);
+    ++launches_;
+    SG_CUDA_TRY(cudaMemcpyAsync(w_.ht_out.ptr, w_.t_out.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    h_->sync();
+    memcpy(out.data(), w_.ht_out.ptr, n * 4);
 }
 
 // Grow the pool to hold `members` candidates.  The workspace buffer may be
@@ -322,7 +346,11 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     uint32_t next_ck = 0;
     std::vector<MNode> wave;
     QuerySet qs, qpool, qfhut, qchild;
-    std::vector<uint32_t> counts, pool_hit, fhut_cnt, tmp;
+    std::vector<uint32_t> counts, counts_q, pool_hit, fhut_cnt, tmp;
+    // tail counts of nodes with a mask: concatenated tails, per-node ranges and slots
+    std::vector<uint64_t> t_ptr;
+    std::vector<uint32_t> t_items, t_slot;
+    std::vector<std::pair<uint8_t, uint64_t>> count_src;   // per wave node: (0 tail path | 1 query path, offset)
     std::vector<float> wfeat, wscore;
     int status = SGFIM_OK;
 
@@ -380,36 +408,49 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                                st, h_->n_sm);
             ++launches_;
         }
-        // ---- phase A: s_e for every tail item
+        // ---- phase A: s_e for every tail item (nodes with a mask: one record per node;
+        // nodes without one, created while the arena was full: a query per item)
         qs.clear();
-        for (const MNode &nd : wave) {
-            for (uint32_t e : nd.tail) {
-                if (nd.slot != kNoSlot) {
-                    qs.add(&e, 1, nd.slot);
-                } else {
+        t_ptr.assign(1, 0);
+        t_items.clear();
+        t_slot.clear();
+        count_src.resize(wave.size());
+        for (size_t i = 0; i < wave.size(); ++i) {
+            const MNode &nd = wave[i];
+            if (nd.slot != kNoSlot) {
+                count_src[i] = {0, t_items.size()};
+                if (nd.tail.empty()) continue;
+                t_items.insert(t_items.end(), nd.tail.begin(), nd.tail.end());
+                t_ptr.push_back(t_items.size());
+                t_slot.push_back(nd.slot);
+            } else {
+                count_src[i] = {1, qs.size()};
+                for (uint32_t e : nd.tail) {
                     tmp.assign(nd.head.begin(), nd.head.end());
                     tmp.push_back(e);
                     qs.add(tmp.data(), tmp.size(), kNoSlot);
                 }
             }
         }
-        timed(0, [&] { run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts); });
+        timed(0, [&] {
+            run_tail_counts(t_ptr, t_items, t_slot, counts);
+            run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts_q);
+        });
         // ---- phase B: PEP, ordering, pool and FHUT queries
         work.assign(wave.size(), Work{});
         qpool.clear();
         qfhut.clear();
-        size_t off = 0;
         for (size_t i = 0; i < wave.size(); ++i) {
             MNode &nd = wave[i];
             Work &wk = work[i];
             wk.head = nd.head;
+            const uint32_t *cs = (count_src[i].first == 0 ? counts.data() : counts_q.data()) + count_src[i].second;
             for (size_t j = 0; j < nd.tail.size(); ++j) {
-                const uint32_t s = counts[off + j];
+                const uint32_t s = cs[j];
                 if (s < thr_) continue;
                 if (s == nd.sup) wk.head.push_back(nd.tail[j]);
                 else wk.f.emplace_back(s, nd.tail[j]);
             }
-            off += nd.tail.size();
             std::sort(wk.f.begin(), wk.f.end());
             tmp.assign(wk.head.begin(), wk.head.end());
             for (auto &pr : wk.f) tmp.push_back(pr.second);

@@ -166,7 +166,11 @@ __global__ void __launch_bounds__(256) query_kernel(QueryBatch qb) {
             const uint64_t w = base + 2 * lane;
             if (w < qb.n_words) {
                 uint4 v = mask ? ld_nc_v4(mask + w) : make_uint4(~0u, ~0u, ~0u, ~0u);
-                for (uint64_t i = a; i < b; ++i) v = and4(v, ld_nc_v4(qb.rows + (uint64_t)qb.q_items[i] * qb.row_stride + w));
+                for (uint64_t i = a; i < b; ++i) {
+                    // once the AND is empty the remaining rows cannot add a bit
+                    if ((v.x | v.y | v.z | v.w) == 0) break;
+                    v = and4(v, ld_nc_v4(qb.rows + (uint64_t)qb.q_items[i] * qb.row_stride + w));
+                }
                 acc += popc4(v);
             }
             if (qb.mode == QUERY_ANY && __any_sync(0xffffffffu, acc != 0)) break;

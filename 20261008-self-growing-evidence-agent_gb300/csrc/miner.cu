@@ -112,6 +112,15 @@ class Miner {
     DevBuf &q_out_, &score_;
     HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
+    // vectors of finished nodes, reused for new children (no allocation per node once warm)
+    std::vector<std::vector<uint32_t>> spare_;
+    std::vector<uint64_t> cand_freq_;   // candidates holding each dense item (pool row density)
+    std::vector<uint32_t> take_spare() {
+        if (spare_.empty()) return {};
+        std::vector<uint32_t> v = std::move(spare_.back());
+        spare_.pop_back();
+        return v;
+    }
     double phase_[6] = {0, 0, 0, 0, 0, 0};   // see sgfim_result.phase_s
     // adds the wall time of f() to phase_[i]
     template <class F> void timed(int i, F &&f) {
@@ -214,14 +223,15 @@ void Miner::pool_reserve(uint64_t members) {
 }
 
 void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node) {
-    std::vector<uint32_t> s(set);
-    std::sort(s.begin(), s.end());
-    citems_.insert(citems_.end(), s.begin(), s.end());
+    const size_t at = citems_.size();
+    citems_.insert(citems_.end(), set.begin(), set.end());
+    std::sort(citems_.begin() + at, citems_.end());
     cptr_.push_back(citems_.size());
     csup_.push_back(sup);
     ctime_.push_back(elapsed());
     cnode_.push_back(node);
     ccheck_.push_back(pool_n_);
+    for (size_t k = at; k < citems_.size(); ++k) ++cand_freq_[citems_[k]];
 }
 
 // Append candidates [from, n) to the device pool (asynchronous; the next
@@ -308,6 +318,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     if (p_.order == SGFIM_ORDER_LEARNED && h_->scorer.in_dim != kDim)
         return fail(h_, SGFIM_EINVAL, "scorer input width must equal SGFIM_TRACE_DIM");
     thr_ = p_.min_count;
+    cand_freq_.assign(ds_.d, 0);
     t0_ = Clock::now();
     cudaStream_t st = h_->stream;
     const uint32_t d = ds_.d;
@@ -363,6 +374,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     };
     std::vector<Work> work;
     std::vector<MNode> kids;
+    std::vector<size_t> ord;
     std::vector<std::pair<uint32_t, uint32_t>> kid_src;  // (parent slot, added item)
     std::vector<uint32_t> child_slot;
 
@@ -376,6 +388,11 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             std::swap(stack, deferred);
         }
         // ---- pop a wave
+        // the previous wave's nodes are done: keep their vectors for the next children
+        for (MNode &nd : wave) {
+            if (nd.head.capacity()) { nd.head.clear(); spare_.push_back(std::move(nd.head)); }
+            if (nd.tail.capacity()) { nd.tail.clear(); spare_.push_back(std::move(nd.tail)); }
+        }
         wave.clear();
         uint64_t nq = 0;
         while (!stack.empty() && wave.size() < nmax) {
@@ -437,7 +454,14 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts_q);
         });
         // ---- phase B: PEP, ordering, pool and FHUT queries
-        work.assign(wave.size(), Work{});
+        // Work records keep their vectors' capacity from wave to wave
+        if (work.size() < wave.size()) work.resize(wave.size());
+        for (size_t i = 0; i < wave.size(); ++i) {
+            work[i].head.clear();
+            work[i].f.clear();
+            work[i].kind = 0;
+            work[i].pool_q = work[i].fhut_q = work[i].kid0 = work[i].nkids = 0;
+        }
         qpool.clear();
         qfhut.clear();
         for (size_t i = 0; i < wave.size(); ++i) {
@@ -455,6 +479,9 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             tmp.assign(wk.head.begin(), wk.head.end());
             for (auto &pr : wk.f) tmp.push_back(pr.second);
             wk.pool_q = qpool.size();
+            // rarest pool rows first: the device AND empties sooner and stops reading rows
+            std::sort(tmp.begin(), tmp.end(),
+                      [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
             qpool.add(tmp.data(), tmp.size(), kNoSlot);
             if (wk.f.empty()) {
                 wk.kind = 0;
@@ -496,7 +523,9 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             wk.nkids = nf;
             for (size_t j = 0; j < nf; ++j) {
                 MNode c;
-                c.head = wk.head;
+                c.head = take_spare();
+                c.tail = take_spare();
+                c.head.assign(wk.head.begin(), wk.head.end());
                 c.head.push_back(wk.f[j].second);
                 c.sup = wk.f[j].first;
                 c.tail.reserve(nf - j - 1);
@@ -549,7 +578,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             // stack is LIFO: nodes pushed later are popped first; keep wave order
             Work &wk = work[i];
             if (wk.kind == 0 || wk.nkids == 0) continue;
-            std::vector<size_t> ord(wk.nkids);
+            ord.resize(wk.nkids);
             std::iota(ord.begin(), ord.end(), wk.kid0);
             if (p_.order == SGFIM_ORDER_SUPPORT_DESC) {
                 std::reverse(ord.begin(), ord.end());
@@ -635,14 +664,17 @@ int Miner::finish(sgfim_result **out) {
         const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
         const uint64_t chunk = 1u << 20;
         QuerySet qs;
-        std::vector<uint32_t> cnt;
+        std::vector<uint32_t> cnt, tmp;
         std::vector<uint64_t> w0;
         for (uint64_t a = 0; a < n; a += chunk) {
             const uint64_t b = std::min(n, a + chunk);
             qs.clear();
             w0.clear();
             for (uint64_t c = a; c < b; ++c) {
-                qs.add(citems_.data() + cptr_[c], cptr_[c + 1] - cptr_[c], kNoSlot);
+                tmp.assign(citems_.begin() + cptr_[c], citems_.begin() + cptr_[c + 1]);
+                std::sort(tmp.begin(), tmp.end(),
+                          [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
+                qs.add(tmp.data(), tmp.size(), kNoSlot);
                 w0.push_back(ccheck_[c] / 64);
             }
             timed(3, [&] { run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_ANY2, cnt, w0.data()); });

@@ -478,19 +478,21 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             std::sort(wk.f.begin(), wk.f.end());
             tmp.assign(wk.head.begin(), wk.head.end());
             for (auto &pr : wk.f) tmp.push_back(pr.second);
-            wk.pool_q = qpool.size();
-            // rarest pool rows first: the device AND empties sooner and stops reading rows
-            std::sort(tmp.begin(), tmp.end(),
-                      [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
-            qpool.add(tmp.data(), tmp.size(), kNoSlot);
             if (wk.f.empty()) {
                 wk.kind = 0;
             } else {
+                // tmp = head, then F: the FHUT query of a masked node takes the F part
                 wk.kind = 1;
                 wk.fhut_q = qfhut.size();
                 if (nd.slot != kNoSlot) qfhut.add(tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
                 else qfhut.add(tmp.data(), tmp.size(), kNoSlot);
             }
+            // the pool query lists the rarest pool rows first: the device AND empties
+            // sooner and stops reading rows
+            std::sort(tmp.begin(), tmp.end(),
+                      [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
+            wk.pool_q = qpool.size();
+            qpool.add(tmp.data(), tmp.size(), kNoSlot);
         }
         if (pool_n_ > 0) {
             const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;

@@ -421,51 +421,28 @@ template <int MW>
 __device__ __forceinline__ void vcount(const uint32_t *tid, const uint32_t *rows, uint32_t vw, uint32_t W,
                                        const Mask<MW> &T, const Mask<MW> &T0, uint32_t *cnt, uint32_t lane) {
     constexpr uint32_t kReg = 4;   // tidsets of up to 128 words stay in registers across the items
-    constexpr int kItems = 4;      // items counted together: their warp reductions overlap
     uint32_t tr[kReg];
     const bool small = W <= 32 * kReg;
 #pragma unroll
     for (uint32_t k = 0; k < kReg; ++k) tr[k] = (small && lane + 32 * k < W) ? tid[lane + 32 * k] : 0u;
-    Mask<MW> x = T;
-    for (;;) {
-        // next (up to) kItems items of T
-        uint32_t e[kItems];
-        int m = 0;
 #pragma unroll
-        for (int q = 0; q < kItems; ++q) {
-            e[q] = 0xffffffffu;
-#pragma unroll
-            for (int ww = 0; ww < MW; ++ww) {
-                if (e[q] == 0xffffffffu && x.w[ww]) {
-                    e[q] = ww * 64 + (__ffsll((long long)x.w[ww]) - 1);
-                    x.w[ww] &= x.w[ww] - 1;
-                }
-            }
-            m += e[q] != 0xffffffffu;
-        }
-        if (m == 0) break;
-        uint32_t acc[kItems];
-#pragma unroll
-        for (int q = 0; q < kItems; ++q) {
-            acc[q] = 0;
-            if (e[q] == 0xffffffffu) continue;
-            const uint32_t *row = rows + (uint64_t)m_rank(T0, e[q]) * vw;
+    for (int ww = 0; ww < MW; ++ww) {
+        uint64_t x = T.w[ww];
+        while (x) {
+            const uint32_t e = ww * 64 + (__ffsll((long long)x) - 1);
+            x &= x - 1;
+            const uint32_t *row = rows + (uint64_t)m_rank(T0, e) * vw;
+            uint32_t acc = 0;
             if (small) {
 #pragma unroll
                 for (uint32_t k = 0; k < kReg; ++k)
-                    if (lane + 32 * k < W) acc[q] += __popc(tr[k] & row[lane + 32 * k]);
+                    if (lane + 32 * k < W) acc += __popc(tr[k] & row[lane + 32 * k]);
             } else {
-                for (uint32_t w = lane; w < W; w += 32) acc[q] += __popc(tid[w] & row[w]);
+                for (uint32_t w = lane; w < W; w += 32) acc += __popc(tid[w] & row[w]);
             }
+            acc = __reduce_add_sync(kFull, acc);
+            if (lane == 0) cnt[e] = acc;
         }
-#pragma unroll
-        for (int q = 0; q < kItems; ++q) acc[q] = __reduce_add_sync(kFull, acc[q]);
-        if (lane == 0) {
-#pragma unroll
-            for (int q = 0; q < kItems; ++q)
-                if (e[q] != 0xffffffffu) cnt[e[q]] = acc[q];
-        }
-        if (m < kItems) break;
     }
     __syncwarp();
 }

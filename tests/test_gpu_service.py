@@ -157,3 +157,24 @@ def test_appends_wait_for_windows_being_mined(engine):
             assert res.as_dict(w) == _oracle_mfis(rows[s:s + L], thr), w
     finally:
         ring.close()
+
+
+def test_mine_windows_wide_ring_uses_wave_miner(engine):
+    """A ring of more than 128 items has no item masks: every window goes to
+    the wave miner, and the results come back as 4-word masks, equal to the
+    oracle's."""
+    from sgfim.service import Ring, masks_to_sets
+    rows = datagen.regime_txns(12_000, 25, 8, 6, 0.3, seed=21)   # 200 items
+    rp, it = datagen.txns_to_csr(rows)
+    ring = Ring(200, 1 << 14)
+    try:
+        ring.append(rp, it)
+        starts, lens = [0, 5000, 11_000], [4000, 7000, 1000]
+        thrs = [max(1, int(np.ceil(0.04 * L))) for L in lens]
+        res = ring.mine_windows(engine, starts, lens, thrs)
+        assert res.mask_words == 4 and not res.batched.any() and (res.status == 0).all()
+        for w, (s, L, t) in enumerate(zip(starts, lens, thrs)):
+            assert res.as_dict(w) == _oracle_mfis(rows[s:s + L], t, d=200), w
+        assert masks_to_sets(np.array([[1, 0, 0, 1 << 3]], np.uint64)) == [(0, 195)]
+    finally:
+        ring.close()

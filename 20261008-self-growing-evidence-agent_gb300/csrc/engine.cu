@@ -421,7 +421,7 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
 
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves) {
     if (!h) return SGFIM_EINVAL;
-    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_STREAM) return fail(h, SGFIM_EINVAL, "unknown kernel");
+    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_STAGED4) return fail(h, SGFIM_EINVAL, "unknown kernel");
     h->plan.kernel = kernel;
     h->plan.cands_per_cta = cands_per_cta;
     h->plan.waves = waves;

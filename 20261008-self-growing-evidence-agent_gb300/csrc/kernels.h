@@ -54,7 +54,9 @@ void launch_tail_counts(const uint64_t *rows, uint64_t row_stride, uint64_t n_wo
 // Batched candidate supports (config "support-1m" path).  Packs CSR candidates
 // into 16-byte records when every item fits 16 bits and k <= 8, runs the
 // shared-memory staged kernel on those and the streaming kernel on the rest.
-enum SupportKernel : int { SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3 };
+enum SupportKernel : int {
+    SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3, SUPPORT_STAGED4 = 4
+};
 struct SupportPlan {
     int kernel = SUPPORT_AUTO;
     uint32_t cands_per_cta = 0;    // 0 = derived from the SM count

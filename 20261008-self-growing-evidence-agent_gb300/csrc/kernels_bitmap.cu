@@ -389,6 +389,119 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// 4-lane transpose-reduce: lane l (of an aligned group of 4) enters with
+// partials p[0..3] for 4 candidates and leaves with the group-wide sum of p[l].
+__device__ __forceinline__ uint32_t treduce4(const uint32_t (&p)[4], uint32_t l) {
+    uint32_t q[2];
+    const bool h2 = l & 2, h1 = l & 1;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t send = h2 ? p[k] : p[k + 2];
+        const uint32_t keep = h2 ? p[k + 2] : p[k];
+        q[k] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    const uint32_t send = h1 ? q[0] : q[1];
+    const uint32_t keep = h1 ? q[1] : q[0];
+    return keep + __shfl_xor_sync(0xffffffffu, send, 1);
+}
+
+// k1_staged_kernel with groups of 4 lanes: each lane ANDs 32 bytes of a row
+// (two 16-byte pieces, 64 bytes apart), so a candidate's record is decoded by
+// 4 lanes instead of 8 and a warp evaluates 8 candidates per step.  Even
+// groups read the row's first half first and odd groups its second half
+// first: the two groups of an 8-lane phase of a 128-bit shared load then hit
+// disjoint banks.
+template <int THREADS, int SMAX>
+__global__ void __launch_bounds__(THREADS, 1)
+    k1_staged4_kernel(const __grid_constant__ CUtensorMap bm_map, uint32_t n_boxes, uint64_t n_words,
+                      const uint4 *__restrict__ recs, uint64_t n_cand, uint32_t cpc, uint32_t *__restrict__ out,
+                      uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr uint32_t G = THREADS / 4;             // groups of 4 lanes
+    uint8_t *chunk = smem;                           // n_boxes * 256 rows * 128 B
+    const uint32_t chunk_bytes = n_boxes * kStagedRowsPerBox * kStagedWords * 8;
+    uint4 *rec_s = reinterpret_cast<uint4 *>(smem + chunk_bytes);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + chunk_bytes + (size_t)cpc * 16);
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t g = tid >> 2, l = tid & 3;
+    const uint32_t off_a = ((g & 1) ? 64u : 0u) + l * 16, off_b = ((g & 1) ? 0u : 64u) + l * 16;
+    const uint64_t base = (uint64_t)blockIdx.x * cpc;
+    if (base >= n_cand) return;
+    const uint64_t left = n_cand - base;
+    const uint32_t ncta = left < cpc ? (uint32_t)left : cpc;
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    for (uint32_t i = tid; i < ncta; i += THREADS) rec_s[i] = recs[base + i];
+    __syncthreads();
+
+    uint32_t acc[SMAX];
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) acc[s] = 0;
+    const uint32_t n_sets = (ncta + 4 * G - 1) / (4 * G);
+    const uint64_t n_chunks = (n_words + kStagedWords - 1) / kStagedWords;
+    uint32_t phase = 0;
+    for (uint64_t ch = 0; ch < n_chunks; ++ch) {
+        if (tid == 0) {
+            mbar_arrive_expect_tx(bar, chunk_bytes);
+            for (uint32_t b = 0; b < n_boxes; ++b)
+                tma_load_2d(chunk + (size_t)b * kStagedRowsPerBox * kStagedWords * 8, &bm_map,
+                            (int32_t)(ch * kStagedWords), (int32_t)(b * kStagedRowsPerBox), bar);
+        }
+        const bool ok = mbar_wait_bounded(bar, phase, err);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            // give in-flight copies one more bounded chance to land before leaving
+            mbar_wait_bounded(bar, phase ^ 1, err);
+            return;
+        }
+#pragma unroll
+        for (int s = 0; s < SMAX; ++s) {
+            if ((uint32_t)s < n_sets) {
+                uint32_t p[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t c = ((uint32_t)s * 4 + j) * G + g;
+                    uint32_t v = 0;
+                    if (c < ncta) {
+                        const uint4 r = rec_s[c];
+                        const uint32_t h[4] = {r.x, r.y, r.z, r.w};
+                        const uint32_t it0 = h[0] & 0xffffu;
+                        if (it0 != kRecNone) {
+                            const uint8_t *row = chunk + (size_t)it0 * 128;
+                            uint4 ma = *reinterpret_cast<const uint4 *>(row + off_a);
+                            uint4 mb = *reinterpret_cast<const uint4 *>(row + off_b);
+#pragma unroll
+                            for (int k = 1; k < 8; ++k) {
+                                const uint32_t it = (h[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+                                if (it == kRecNone) break;
+                                const uint8_t *rk = chunk + (size_t)it * 128;
+                                ma = and4(ma, *reinterpret_cast<const uint4 *>(rk + off_a));
+                                mb = and4(mb, *reinterpret_cast<const uint4 *>(rk + off_b));
+                            }
+                            v = popc4(ma) + popc4(mb);
+                        }
+                    }
+                    p[j] = v;
+                }
+                acc[s] += treduce4(p, l);
+            }
+        }
+        __syncthreads();  // every group is done with this chunk before TMA overwrites it
+    }
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) {
+        const uint32_t c = ((uint32_t)s * 4 + l) * G + g;
+        if ((uint32_t)s < n_sets && c < ncta) {
+            const uint32_t it0 = rec_s[c].x & 0xffffu;
+            if (it0 != kRecNone) out[base + c] = acc[s];
+        }
+    }
+}
+
 // ---------------------------------------------------------------- sorted batch supports
 // Candidates are counting-sorted by key = (k - 1) * 4096 + first item, so that
 // (a) the four 8-lane groups of a warp almost always share k and run one fully
@@ -607,6 +720,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 constexpr int kStagedThreads = 1024;
 constexpr int kStagedSmax = 8;
+constexpr int kStagedSmax4 = 8;   // 4-lane groups: 8 sets x 4 candidates x 256 groups = 8,192
 constexpr int kSortedSmax = 8;
 constexpr uint32_t kSortedMaxCpc = kStagedThreads / 8 * 8 * kSortedSmax;  // 8192
 
@@ -674,12 +788,12 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     // (depending on its grid); the staged kernel is the default, the sorted one a tuning option
     if (kind == SUPPORT_AUTO) kind = SUPPORT_STAGED;
     if (kind == SUPPORT_SORTED && d > kSortCompactMax) kind = SUPPORT_STAGED;
-    if (kind == SUPPORT_STAGED && d > 65535) kind = SUPPORT_STREAM;
+    if ((kind == SUPPORT_STAGED || kind == SUPPORT_STAGED4) && d > 65535) kind = SUPPORT_STREAM;
     uint32_t cpc = 0;
     if (kind == SUPPORT_SORTED) {
         cpc = pick_cpc(kSortedMaxCpc, sorted_smem_bytes, 1);
         if (!cpc) kind = SUPPORT_STREAM;
-    } else if (kind == SUPPORT_STAGED) {
+    } else if (kind == SUPPORT_STAGED || kind == SUPPORT_STAGED4) {
         cpc = pick_cpc(kStagedMaxCpc, staged_smem_bytes, 2);
         if (!cpc) kind = SUPPORT_STREAM;
     }
@@ -733,7 +847,8 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
                                                          out);
         SG_CUDA_TRY(cudaGetLastError());
         const size_t smem = staged_smem_bytes(d, cpc);
-        auto kern = k1_staged_kernel<kStagedThreads, kStagedSmax>;
+        auto kern = kind == SUPPORT_STAGED4 ? k1_staged4_kernel<kStagedThreads, kStagedSmax4>
+                                            : k1_staged_kernel<kStagedThreads, kStagedSmax>;
         SG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         mark(1);
         kern<<<(unsigned)ctas, kStagedThreads, smem, st>>>(*map, n_boxes, n_words_even, recs, n_cand, cpc, out,

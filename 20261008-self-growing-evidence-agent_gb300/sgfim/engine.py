@@ -204,7 +204,7 @@ class Engine:
         self._check(self._L.sgfim_support_batch_device(self._h, bm_ptr, d, n_words, row_stride, cand_ptr_ptr,
                                                        cand_items_ptr, n_cand, out_ptr, stream or None))
 
-    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3}
+    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3, "staged4": 4}
 
     def set_support_plan(self, kernel="auto", cands_per_cta=0, waves=0):
         """Choose the support-batch kernel and its CTA sizing (see sgfim_support_plan_set)."""

@@ -54,7 +54,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cooc", action="store_true")
-    ap.add_argument("--kernel", choices=["auto", "sorted", "staged", "stream"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "sorted", "staged", "staged4", "stream"], default="auto")
     return ap.parse_args()
 
 
@@ -262,6 +262,7 @@ def main():
     peaks, peak_src = measured_peaks()
     achieved = alg_bytes / (count_ms / 1000.0) / 1e9
     kname = {"auto": "k1_staged_kernel", "sorted": "k1_sorted_kernel", "staged": "k1_staged_kernel",
+             "staged4": "k1_staged4_kernel",
              "stream": "query_kernel"}[args.kernel]
     tr = ncu_traffic(kname.replace("_kernel", ""))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",

@@ -150,6 +150,7 @@ int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
 #define SGFIM_KERNEL_STAGED 1  /* TMA-staged chunks, candidates in input order */
 #define SGFIM_KERNEL_SORTED 2  /* TMA-staged chunks, candidates sorted by (k, first item); ids < 1024 */
 #define SGFIM_KERNEL_STREAM 3  /* one warp per candidate, rows streamed from L2/HBM */
+#define SGFIM_KERNEL_STAGED4 4 /* TMA-staged chunks, 4-lane groups (32 bytes of a row per lane) */
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves);
 
 /* Allocation-free form of sgfim_support_batch_device.  It has no counterpart

@@ -27,7 +27,7 @@ def test_autotune_support_and_cooc(engine, tmp_path):
     try:
         tuner = Autotuner(engine, cache)
         best, ms = tuner.tune_support(tb, d, w, w, tp, ti, len(cp) - 1, out)
-        assert len(ms) >= 4 and best[0] in ("staged", "sorted", "stream")
+        assert len(ms) >= 4 and best[0] in ("staged", "staged4", "sorted", "stream")
         assert np.array_equal(out.cpu().numpy().view(np.uint32), oracle.support_batch(bm, cp, ci))
         co = torch.zeros(d * d, dtype=torch.int32, device=dev)
         kind, cms = tuner.tune_cooc(tb, d, w, w, co)

@@ -261,7 +261,7 @@ def main():
     count_ms = ps["count_ms"] / max(1, ps["calls"])
     peaks, peak_src = measured_peaks()
     achieved = alg_bytes / (count_ms / 1000.0) / 1e9
-    kname = {"auto": "k1_staged_kernel", "sorted": "k1_sorted_kernel", "staged": "k1_staged_kernel",
+    kname = {"auto": "k1_staged4_kernel", "sorted": "k1_sorted_kernel", "staged": "k1_staged_kernel",
              "staged4": "k1_staged4_kernel",
              "stream": "query_kernel"}[args.kernel]
     tr = ncu_traffic(kname.replace("_kernel", ""))

@@ -146,7 +146,7 @@ int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
  * kernel: SGFIM_KERNEL_*; cands_per_cta: candidates a CTA owns (0 = derived);
  * waves: CTAs per SM over the grid when cands_per_cta is 0 (0 = the kernel's
  * default: 1 for SORTED, 2 for STAGED). */
-#define SGFIM_KERNEL_AUTO 0    /* staged when it fits shared memory, else streaming */
+#define SGFIM_KERNEL_AUTO 0    /* STAGED4 when it fits shared memory, else streaming */
 #define SGFIM_KERNEL_STAGED 1  /* TMA-staged chunks, candidates in input order */
 #define SGFIM_KERNEL_SORTED 2  /* TMA-staged chunks, candidates sorted by (k, first item); ids < 1024 */
 #define SGFIM_KERNEL_STREAM 3  /* one warp per candidate, rows streamed from L2/HBM */

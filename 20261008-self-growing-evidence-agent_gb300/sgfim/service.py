@@ -475,9 +475,11 @@ def main(argv=None):
                     help="instead of the timed service, mine every request's window in one "
                          "sgfim_ring_mine_windows call, REPEAT times (capacity of the batched miner)")
     ap.add_argument("--horizontal", action="store_true", help="batched miner on horizontal masks")
+    ap.add_argument("--rate", type=float, default=WORKLOAD["rate_hz"],
+                    help="Poisson arrival rate of the requests (req/s); the workload's is 2,000")
     a = ap.parse_args(argv)
-    rows = stream_rows_for(a.requests)
-    reqs = make_requests(a.requests, WORKLOAD["rate_hz"], WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
+    rows = stream_rows_for(a.requests, rate_hz=a.rate)
+    reqs = make_requests(a.requests, a.rate, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
     if a.saturate:
         return saturate(rows, reqs, a.saturate, a.horizontal, int(a.hbm_budget_gb * (1 << 30)), a.out)
     svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
@@ -494,7 +496,7 @@ def main(argv=None):
     for rq in done:
         if rq.error:
             errs[rq.error] = errs.get(rq.error, 0) + 1
-    report = {"workload": "windows-4096", "requests": a.requests,
+    report = {"workload": "windows-4096", "requests": a.requests, "rate_hz": a.rate,
               "workers": a.workers if a.mode == "workers" else 1,
               "hbm_budget_gb": a.hbm_budget_gb, **rep, "error_kinds": errs,
               "config": {k: WORKLOAD[k] for k in WORKLOAD}}

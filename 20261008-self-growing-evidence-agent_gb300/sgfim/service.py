@@ -199,8 +199,8 @@ class WindowView:
 
 class WindowService:
     """mode "batched": one scheduler thread hands every queued request to one
-    sgfim_ring_mine_windows launch (one warp per window; the handle's HBM
-    budget bounds the per-warp workspaces and the output arena).  mode
+    sgfim_ring_mine_windows call (a warp per root subtree of every window; the
+    handle's HBM budget bounds the per-warp workspaces and the output arena).  mode
     "workers": `workers` threads, each with its own handle, mine one window at
     a time with the wave miner, admitted by a per-window memory estimate."""
 

@@ -330,14 +330,19 @@ int sgfim_ring_append(sgfim_ring *r, const uint64_t *row_ptr, const uint32_t *it
  * in the ring: head - start <= capacity and start + len <= head. */
 int sgfim_ring_window_load(sgfim_ring *r, sgfim_handle *h, uint64_t start, uint64_t len);
 
-/* MFIs of many windows of the ring in one persistent launch (no reference
+/* MFIs of many windows of the ring in a few batched launches (no reference
  * counterpart: the reference runs one engine process per window file).
  * Window w is [starts[w], starts[w] + lens[w]) at absolute floor
- * min_counts[w] (0 is taken as 1); its result equals sgfim_mine on
- * sgfim_ring_window_load of the same window.  One warp mines one window
- * (rings of at most 128 items); a window that outgrows the warp's workspace,
- * or any window of a wider ring, is mined by the wave miner on `h` instead,
- * so `h`'s dataset is replaced.  Appends from other threads may proceed
+ * min_counts[w] (0 is taken as 1); its result (as a set) equals sgfim_mine on
+ * sgfim_ring_window_load of the same window.  Rings of at most 128 items:
+ * each window's root is expanded on the device and every root subtree (the
+ * costliest ones split once more) is searched by one warp, all tasks of all
+ * windows in one persistent launch; a cross-subtree filter and a device
+ * gather then produce each window's MFIs, listed in depth-first order.  A
+ * window whose task outgrows its warp's workspace, and every window of a
+ * wider ring, is mined by the wave miner on `h` instead, so `h`'s dataset is
+ * replaced.  The handle's HBM budget bounds the per-warp workspaces (half)
+ * and the output arena (a quarter).  Appends from other threads may proceed
  * meanwhile; an append that would overwrite a window still being mined waits
  * for it. */
 typedef struct sgfim_windows_result {

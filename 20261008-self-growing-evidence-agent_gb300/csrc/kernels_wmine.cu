@@ -892,7 +892,15 @@ template <int MW> __global__ void __launch_bounds__(128) wtask_kernel(WMineParam
     }
 }
 
-template <int MW> __global__ void __launch_bounds__(128, 6) wvtask_kernel(WMineParams p) {
+// Resident CTAs per SM the register allocation is fitted to.  Measured on the
+// 4,096 service windows: 6 (80 registers, 3,648 warps) 337 ms, 7 (72 registers,
+// 4,176 warps, the workspace budget's limit) 338 ms with a longer makespan, 8
+// (64 registers, spills) 358 ms -- more resident warps do not shorten the search.
+#ifndef SGFIM_WVTASK_MIN_BLOCKS
+#define SGFIM_WVTASK_MIN_BLOCKS 6
+#endif
+
+template <int MW> __global__ void __launch_bounds__(128, SGFIM_WVTASK_MIN_BLOCKS) wvtask_kernel(WMineParams p) {
     __shared__ uint32_t s_cnt[4][128];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t wib = threadIdx.x >> 5;

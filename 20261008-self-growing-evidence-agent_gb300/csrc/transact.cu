@@ -110,6 +110,22 @@ __global__ void quantile_kernel(const double *__restrict__ stats, uint32_t R, co
     edges[i] = v;
 }
 
+// numpy's median of `window` consecutive values (insertion sort while loading;
+// the mean of the two middle values for an even count).
+__device__ __forceinline__ double window_median(const double *__restrict__ col, uint32_t window) {
+    double buf[kMaxWindow];
+    for (uint32_t j = 0; j < window; ++j) {
+        const double v = col[j];
+        uint32_t k = j;
+        while (k > 0 && buf[k - 1] > v) {
+            buf[k] = buf[k - 1];
+            --k;
+        }
+        buf[k] = v;
+    }
+    return (window & 1) ? buf[window / 2] : __ddiv_rn(__dadd_rn(buf[window / 2 - 1], buf[window / 2]), 2.0);
+}
+
 // One thread per (window, sensor): median of the window's values, binned.
 __global__ void window_bin_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t window,
                                   uint32_t stride, uint64_t n_win, const double *__restrict__ edges,
@@ -121,19 +137,7 @@ __global__ void window_bin_kernel(const double *__restrict__ cols, uint64_t n, u
     const uint64_t w = i / S;
     const uint32_t s = (uint32_t)(i - w * S);
     const uint64_t start = w * stride;
-    const double *col = cols + (uint64_t)s * n + start;
-    double buf[kMaxWindow];
-    for (uint32_t j = 0; j < window; ++j) {
-        // insertion sort while loading
-        const double v = col[j];
-        uint32_t k = j;
-        while (k > 0 && buf[k - 1] > v) {
-            buf[k] = buf[k - 1];
-            --k;
-        }
-        buf[k] = v;
-    }
-    const double med = (window & 1) ? buf[window / 2] : __ddiv_rn(__dadd_rn(buf[window / 2 - 1], buf[window / 2]), 2.0);
+    const double med = window_median(cols + (uint64_t)s * n + start, window);
     const double *e = edges + (uint64_t)s * edge_stride;
     const uint32_t m = n_edges[s];
     uint32_t cnt = 0;   // edges <= med (searchsorted side="right")
@@ -152,11 +156,265 @@ __global__ void window_bin_kernel(const double *__restrict__ cols, uint64_t n, u
     }
 }
 
+// ---------------------------------------------------------------- online (P²) edges
+//
+// code/pipeline/online_discretize.py: every sensor keeps n_bins-1 five-marker
+// estimators (P2Quantile :22-71) at quantiles i/n_bins; run_file (:111-128)
+// feeds every row of every window, in window order, to every estimator (rows
+// shared by overlapping windows are fed again) and after each window bins the
+// window median with the edges of that moment (OnlineBinner.edges :87-103).
+// The estimator is a sequential recurrence, so the parallel axis is (sensor,
+// estimator); each one runs on lane 0 of its own warp, so that the warps spread
+// over the SMs' schedulers and every double operation of the chain issues at
+// once.  All arithmetic is explicitly rounded (no fused multiply-add), in the
+// reference's order, so the estimates are the reference's bit for bit.
+
+constexpr uint32_t kMaxOnlineBins = 64;
+
+// stable insertion sort of five registers (Python's sorted on equal keys)
+__device__ __forceinline__ void sort5(double (&a)[5]) {
+#pragma unroll
+    for (int i = 1; i < 5; ++i)
+#pragma unroll
+        for (int j = i; j > 0; --j)
+            if (a[j - 1] > a[j]) {
+                const double t = a[j - 1];
+                a[j - 1] = a[j];
+                a[j] = t;
+            }
+}
+
+// est[(w * S + s) * m + j] = estimate j of sensor s after window w
+__global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t m,
+                                                 const double *__restrict__ quant, uint32_t window, uint32_t stride,
+                                                 uint64_t n_win, double *__restrict__ est) {
+    const uint64_t e = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    if ((threadIdx.x & 31) != 0 || e >= (uint64_t)S * m) return;
+    const uint32_t s = (uint32_t)(e / m), j = (uint32_t)(e - (uint64_t)s * m);
+    const double q = quant[j];
+    const double *col = cols + (uint64_t)s * n;
+    double qv[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    double np_[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    uint32_t n_init = 0;
+    for (uint64_t w = 0; w < n_win; ++w) {
+        const uint64_t start = w * stride;
+        for (uint32_t t = 0; t < window; ++t) {
+            const double x = col[start + t];
+            if (n_init < 5) {
+#pragma unroll
+                for (int i = 0; i < 5; ++i)
+                    if ((uint32_t)i == n_init) qv[i] = x;
+                if (++n_init == 5) {
+                    sort5(qv);
+                    np_[0] = 0.0;
+                    np_[1] = __dadd_rn(1.0, __dmul_rn(2.0, q));
+                    np_[2] = __dadd_rn(1.0, __dmul_rn(4.0, q));
+                    np_[3] = __dadd_rn(3.0, __dmul_rn(2.0, q));
+                    np_[4] = 4.0;
+                }
+                continue;
+            }
+            int k;
+            if (x < qv[0]) {
+                qv[0] = x;
+                k = 0;
+            } else if (x < qv[1]) {
+                k = 0;
+            } else if (x < qv[2]) {
+                k = 1;
+            } else if (x < qv[3]) {
+                k = 2;
+            } else if (x <= qv[4]) {
+                k = 3;
+            } else {
+                qv[4] = x;
+                k = 3;
+            }
+#pragma unroll
+            for (int i = 0; i < 5; ++i) np_[i] = __dadd_rn(np_[i], 1.0);
+#pragma unroll
+            for (int i = 1; i < 4; ++i)
+                if (i <= k) np_[i] = __dadd_rn(np_[i], 1.0);
+#pragma unroll
+            for (int i = 1; i < 4; ++i) {
+                const double d = __dsub_rn(np_[i], np_[i - 1]);
+                const double span = __dsub_rn(np_[i + 1], np_[i - 1]);
+                if (d >= 1.0 && span > 1.0) {
+                    const double qp = __ddiv_rn(__dmul_rn(__dadd_rn(d, 1.0), __dsub_rn(qv[i + 1], qv[i - 1])), span);
+                    const double moved = __dadd_rn(qv[i], qp);
+                    if (qv[i - 1] < moved && moved < qv[i + 1]) qv[i] = moved;
+                }
+            }
+        }
+        double v;
+        if (n_init >= 5) {
+            v = qv[2];
+        } else {
+            // fewer than five samples: numpy's median of them (unused slots sort last)
+            double a[5];
+#pragma unroll
+            for (int i = 0; i < 5; ++i) a[i] = (uint32_t)i < n_init ? qv[i] : __longlong_as_double(0x7ff0000000000000ll);
+            sort5(a);
+            v = a[0];
+#pragma unroll
+            for (int i = 1; i < 5; ++i)
+                if ((uint32_t)i == n_init / 2) v = (n_init & 1) ? a[i] : __ddiv_rn(__dadd_rn(a[i - 1], a[i]), 2.0);
+        }
+        est[(w * S + s) * m + j] = v;
+    }
+}
+
+// One thread per (window, sensor): edges from the sensor's estimates after the
+// window, then the window median binned with them.
+__global__ void online_bin_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t window,
+                                  uint32_t stride, uint64_t n_win, const double *__restrict__ est, uint32_t n_bins,
+                                  const int32_t *__restrict__ anomaly, double *__restrict__ edges,
+                                  uint32_t *__restrict__ items, int32_t *__restrict__ labels) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n_win * S) return;
+    const uint64_t w = i / S;
+    const uint32_t s = (uint32_t)(i - w * S);
+    const uint32_t m = n_bins - 1;
+    double q[kMaxOnlineBins - 1];
+    const double *src = est + i * m;
+    for (uint32_t j = 0; j < m; ++j) {
+        const double v = src[j];
+        uint32_t k = j;
+        while (k > 0 && q[k - 1] > v) {
+            q[k] = q[k - 1];
+            --k;
+        }
+        q[k] = v;
+    }
+    double span = __dsub_rn(q[m - 1], q[0]);
+    if (1e-9 > span) span = 1e-9;   // max(q[-1] - q[0], 1e-9)
+    const double min_gap = __dmul_rn(0.05, span);
+    if (n_bins == 3) {
+        if (__dsub_rn(q[1], q[0]) < min_gap) {
+            const double mid = __ddiv_rn(__dadd_rn(q[0], q[1]), 2.0);
+            const double half = __ddiv_rn(min_gap, 2.0);
+            q[0] = __dsub_rn(mid, half);
+            q[1] = __dadd_rn(mid, half);
+        }
+    } else {
+        for (uint32_t j = 1; j < m; ++j) {
+            const double lo = __dadd_rn(q[j - 1], min_gap);
+            if (q[j] < lo) q[j] = lo;
+        }
+    }
+    double *e = edges + i * (n_bins + 1);
+    e[0] = __dsub_rn(q[0], span);
+    for (uint32_t j = 0; j < m; ++j) e[1 + j] = q[j];
+    e[n_bins] = __dadd_rn(q[m - 1], span);
+    const uint64_t start = w * stride;
+    const double med = window_median(cols + (uint64_t)s * n + start, window);
+    uint32_t cnt = 0;   // edges <= med (searchsorted side="right")
+    for (uint32_t j = 0; j <= n_bins; ++j) cnt += e[j] <= med;
+    int32_t b = (int32_t)cnt - 1;
+    if (b < 0) b = 0;
+    if (b > (int32_t)n_bins - 1) b = (int32_t)n_bins - 1;
+    items[i] = s * n_bins + (uint32_t)b;
+    if (s == 0) {
+        int32_t mx = 0;
+        if (anomaly) {
+            mx = anomaly[start];
+            for (uint32_t j = 1; j < window; ++j) mx = max(mx, anomaly[start + j]);
+        }
+        labels[w] = mx;
+    }
+}
+
 }  // namespace
 
 }  // namespace sg
 
 using namespace sg;
+
+extern "C" int sgfim_transactionize_online(sgfim_handle *h, const double *values, uint64_t n_rows,
+                                           uint32_t n_sensors, const int32_t *anomaly, uint32_t window,
+                                           uint32_t stride, uint32_t n_bins, uint32_t flags, double *edges_out,
+                                           uint32_t *items_out, int32_t *labels_out, uint64_t *n_windows_out) {
+    if (!h) return SGFIM_EINVAL;
+    if (!values && n_rows) return fail(h, SGFIM_EINVAL, "null values");
+    if (n_sensors == 0 || window < 1 || stride < 1)
+        return fail(h, SGFIM_EINVAL, "n_sensors, window and stride must be >= 1");
+    if (n_bins < 2 || n_bins > kMaxOnlineBins) return fail(h, SGFIM_EINVAL, "n_bins must be in 2..64");
+    if (window > kMaxWindow) return fail(h, SGFIM_EINVAL, "window longer than 256 rows");
+    if ((uint64_t)n_sensors * n_bins > 0xffffffffull) return fail(h, SGFIM_EINVAL, "too many items");
+    const uint64_t n_win = n_rows >= window ? (n_rows - window) / stride + 1 : 0;
+    if (n_windows_out) *n_windows_out = n_win;
+    if (n_win && (!items_out || !labels_out)) return fail(h, SGFIM_EINVAL, "null output");
+    if ((n_win * n_sensors + 127) / 128 > 0x7fffffffull) return fail(h, SGFIM_EINVAL, "too many windows");
+    API_GUARD_BEGIN
+    SG_CUDA_TRY(cudaSetDevice(h->device));
+    cudaStream_t st = h->stream;
+    const uint32_t S = n_sensors, m = n_bins - 1;
+    DevBuf d_rows, d_cols, d_est, d_out, d_anom;
+    struct Free {
+        DevBuf *b[5];
+        ~Free() {
+            for (DevBuf *x : b) x->release();
+        }
+    } guard{{&d_rows, &d_cols, &d_est, &d_out, &d_anom}};
+    if (n_win) {
+        const size_t mat = (size_t)n_rows * S * 8;
+        d_rows.reserve(mat, st);
+        d_cols.reserve(mat, st);
+        // out: nan count | quantiles | labels | items | edges
+        size_t off = 0;
+        auto carve = [&](size_t bytes) {
+            const size_t o = off;
+            off += (bytes + 255) & ~(size_t)255;
+            return o;
+        };
+        const size_t o_nan = carve(4), o_q = carve((size_t)m * 8), o_lab = carve(n_win * 4),
+                     o_items = carve(n_win * S * 4), o_edges = carve(n_win * S * (n_bins + 1) * 8);
+        d_out.reserve(off, st);
+        d_est.reserve(n_win * S * m * 8, st);
+        char *base = d_out.as<char>();
+        std::vector<double> quant(m);
+        for (uint32_t j = 0; j < m; ++j) quant[j] = (double)(j + 1) / (double)n_bins;   // i / n_bins
+        SG_CUDA_TRY(cudaMemcpyAsync(d_rows.ptr, values, mat, cudaMemcpyHostToDevice, st));
+        SG_CUDA_TRY(cudaMemsetAsync(base + o_nan, 0, 4, st));
+        SG_CUDA_TRY(cudaMemcpyAsync(base + o_q, quant.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+        const uint64_t total = n_rows * S;
+        to_columns_kernel<<<(unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)h->n_sm * 32), 256, 0, st>>>(
+            d_rows.as<double>(), n_rows, S, d_cols.as<double>(), reinterpret_cast<uint32_t *>(base + o_nan));
+        SG_CUDA_TRY(cudaGetLastError());
+        uint32_t nan_count = 0;
+        SG_CUDA_TRY(cudaMemcpyAsync(&nan_count, base + o_nan, 4, cudaMemcpyDeviceToHost, st));
+        SG_CUDA_TRY(cudaStreamSynchronize(st));
+        if (nan_count) return fail(h, SGFIM_EINVAL, "the stream holds NaN values");
+        const uint64_t n_est = (uint64_t)S * m;
+        p2_kernel<<<(unsigned)((n_est + 3) / 4), 128, 0, st>>>(d_cols.as<double>(), n_rows, S, m,
+                                                              reinterpret_cast<const double *>(base + o_q), window,
+                                                              stride, n_win, d_est.as<double>());
+        SG_CUDA_TRY(cudaGetLastError());
+        if (anomaly) {
+            d_anom.reserve(n_rows * 4, st);
+            SG_CUDA_TRY(cudaMemcpyAsync(d_anom.ptr, anomaly, n_rows * 4, cudaMemcpyHostToDevice, st));
+        }
+        const uint64_t nt = n_win * S;
+        online_bin_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(
+            d_cols.as<double>(), n_rows, S, window, stride, n_win, d_est.as<double>(), n_bins,
+            anomaly ? d_anom.as<int32_t>() : nullptr, reinterpret_cast<double *>(base + o_edges),
+            reinterpret_cast<uint32_t *>(base + o_items), reinterpret_cast<int32_t *>(base + o_lab));
+        SG_CUDA_TRY(cudaGetLastError());
+        h->launches += 3;
+        SG_CUDA_TRY(cudaMemcpyAsync(items_out, base + o_items, nt * 4, cudaMemcpyDeviceToHost, st));
+        SG_CUDA_TRY(cudaMemcpyAsync(labels_out, base + o_lab, n_win * 4, cudaMemcpyDeviceToHost, st));
+        if (edges_out)
+            SG_CUDA_TRY(cudaMemcpyAsync(edges_out, base + o_edges, nt * (n_bins + 1) * 8, cudaMemcpyDeviceToHost, st));
+        SG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    if (flags & SGFIM_TX_LOAD) {
+        std::vector<uint64_t> rp(n_win + 1);
+        for (uint64_t w = 0; w <= n_win; ++w) rp[w] = w * S;
+        return sgfim_load_csr(h, rp.data(), items_out, n_win);
+    }
+    return SGFIM_OK;
+    API_GUARD_END(h)
+}
 
 extern "C" int sgfim_transactionize(sgfim_handle *h, const double *values, uint64_t n_rows, uint32_t n_sensors,
                                     const int32_t *anomaly, uint32_t window, uint32_t stride, uint32_t n_bins,

@@ -120,6 +120,9 @@ SIGNATURES = {
     "sgfim_transactionize": (C.c_int, [C.c_void_p, f64p, C.c_uint64, C.c_uint32, C.POINTER(C.c_int32), C.c_uint32,
                                        C.c_uint32, C.c_uint32, C.c_uint32, f64p, u32p, u32p, C.POINTER(C.c_int32),
                                        u64p]),
+    "sgfim_transactionize_online": (C.c_int, [C.c_void_p, f64p, C.c_uint64, C.c_uint32, C.POINTER(C.c_int32),
+                                              C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, f64p, u32p,
+                                              C.POINTER(C.c_int32), u64p]),
     "sgfim_support_batch_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
                                               C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),

@@ -169,6 +169,35 @@ class Engine:
         e = [edges[s * (n_bins + 1):s * (n_bins + 1) + int(n_edges[s])].copy() for s in range(S)]
         return items[:n_win * S].reshape(n_win, S).astype(np.int64), labels[:n_win].astype(np.int64), e
 
+    def transactionize_online(self, values, window=30, stride=15, n_bins=3, anomaly=None, load=False,
+                              with_edges=True):
+        """Online form (P² edges per window, sgfim_transactionize_online):
+        -> (items [n_windows, n_sensors] dense ids, labels [n_windows], edges
+        [n_windows, n_sensors, n_bins+1] or None without ``with_edges``)."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        if values.ndim != 2:
+            raise ValueError("values must be [n_rows, n_sensors]")
+        n, S = values.shape
+        an = None
+        if anomaly is not None:
+            an = np.ascontiguousarray(anomaly, dtype=np.int32)
+            if an.shape != (n,):
+                raise ValueError("one anomaly flag per row")
+        n_win = (n - window) // stride + 1 if n >= window and window >= 1 and stride >= 1 else 0
+        edges = np.zeros((max(1, n_win), S, max(n_bins, 0) + 1), np.float64) if with_edges else None
+        items = np.zeros(max(1, n_win * S), np.uint32)
+        labels = np.zeros(max(1, n_win), np.int32)
+        nw = C.c_uint64(0)
+        rc = self._L.sgfim_transactionize_online(
+            self._h, _p(values, C.c_double), n, S,
+            an.ctypes.data_as(C.POINTER(C.c_int32)) if an is not None else None, window, stride, n_bins,
+            L.TX_LOAD if load else 0, _p(edges, C.c_double) if with_edges else None, _p(items, C.c_uint32),
+            labels.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(nw))
+        self._check(rc)
+        assert nw.value == n_win
+        return (items[:n_win * S].reshape(n_win, S).astype(np.int64), labels[:n_win].astype(np.int64),
+                edges[:n_win] if with_edges else None)
+
     def load_bitmaps(self, bm, n_txn):
         bm = np.ascontiguousarray(bm, dtype=np.uint64)
         d, w = bm.shape

@@ -55,6 +55,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cooc", action="store_true")
     ap.add_argument("--kernel", choices=["auto", "sorted", "staged", "staged4", "stream"], default="auto")
+    ap.add_argument("--workload", choices=["support-1m", "transact-1m"], default="support-1m",
+                    help="transact-1m: the sensor-stream front end (quantile and online P2 "
+                         "transactionisation of 1M-row streams) instead of the support bench")
     return ap.parse_args()
 
 
@@ -192,11 +195,64 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+TRANSACT_STREAMS = [(1_000_000, 8, 3), (1_000_000, 21, 6)]   # rows, sensors, bins; window 30, stride 15
+
+
+def run_transact(args, rank):
+    """--workload transact-1m: sgfim_transactionize and sgfim_transactionize_online
+    on seeded 1M-row streams (host values in, items/edges out, every call
+    timed whole), beside the C restatement of the online discretiser on every
+    host core and on one.  Prints one JSON line per stream (rank 0)."""
+    if rank != 0:
+        return
+    import oracle
+    from sgfim.engine import Engine
+    threads = os.cpu_count() or 1
+    with Engine() as eng:
+        for n, S, nb in TRANSACT_STREAMS:
+            vals, anom = datagen.sensor_stream(n, S, 5)
+            for _ in range(max(1, args.warmup)):
+                eng.transactionize(vals[:100_000], 30, 15, nb, anomaly=anom[:100_000])
+                eng.transactionize_online(vals[:20_000], 30, 15, nb, anomaly=anom[:20_000])
+            t_off, t_on = [], []
+            for _ in range(max(1, min(args.steps, 3))):
+                t = time.perf_counter()
+                eng.transactionize(vals, 30, 15, nb, anomaly=anom)
+                t_off.append(time.perf_counter() - t)
+                t = time.perf_counter()
+                items, labels, edges = eng.transactionize_online(vals, 30, 15, nb, anomaly=anom)
+                t_on.append(time.perf_counter() - t)
+            t = time.perf_counter()
+            w_edges, w_items, _ = oracle.online_bins(vals, 30, 15, nb, anom, n_threads=threads)
+            c_all = time.perf_counter() - t
+            t = time.perf_counter()
+            oracle.online_bins(vals, 30, 15, nb, anom, n_threads=1)
+            c_one = time.perf_counter() - t
+            same = bool(np.array_equal(items, w_items) and np.array_equal(edges.view(np.int64), w_edges.view(np.int64)))
+            on_s = min(t_on)
+            line = {"metric": "rows/s (online P2 transactionisation)", "value": n / on_s, "unit": "rows/s",
+                    "n_gpus": 1, "steps": len(t_on), "warmup": args.warmup, "ms_per_step": 1000 * on_s,
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic (seeded sensor stream)",
+                    "config": {"workload": "transact-1m", "rows": n, "sensors": S, "bins": nb, "window": 30,
+                               "stride": 15, "windows": int(items.shape[0])},
+                    "offline_quantile_call_s": min(t_off), "online_call_s": on_s, "matches_c_oracle": same,
+                    "cpu_baseline": {"value": n / c_all, "unit": "rows/s", "cores": threads, "kind": "port",
+                                     "sample": f"whole stream, C restatement, {threads} threads ({c_all:.2f} s; "
+                                               f"1 thread {c_one:.2f} s)"},
+                    "e2e": {"value": n / on_s, "unit": "rows/s", "h2d_bytes_per_step": int(vals.nbytes + anom.nbytes),
+                            "d2h_bytes_per_step": int(items.size * 4 + labels.size * 4 + edges.nbytes)},
+                    "gpu_launches": 3}
+            print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "transact-1m":
+        return run_transact(args, rank)
     if args.impl == "reference":
         return run_reference(args, rank, world)
 

@@ -387,6 +387,22 @@ int sgfim_transactionize(sgfim_handle *h, const double *values, uint64_t n_rows,
                          double *edges_out, uint32_t *n_edges_out, uint32_t *items_out, int32_t *labels_out,
                          uint64_t *n_windows_out);
 
+/* The online (streaming) form of the same transactions
+ * (code/pipeline/online_discretize.py: P2Quantile :22-71, OnlineBinner
+ * :74-103, bin_index :106-108, run_file :111-128).  Every sensor keeps
+ * n_bins-1 five-marker P² estimators at i/n_bins; every row of every window,
+ * in window order, is fed to them (rows of overlapping windows are fed again),
+ * and after each window its median is binned with the edges of that moment:
+ * edges_out[(w * n_sensors + s) * (n_bins+1) ..] (nullable: not copied back),
+ * items_out[w * n_sensors + s] = s * n_bins + bin, labels_out[w] as in
+ * sgfim_transactionize.  Windows as in sgfim_transactionize; a stream shorter
+ * than one window gives 0 windows and SGFIM_OK.  2 <= n_bins <= 64, window <=
+ * 256, NaN-free values (EINVAL otherwise).  SGFIM_TX_LOAD as above. */
+int sgfim_transactionize_online(sgfim_handle *h, const double *values, uint64_t n_rows, uint32_t n_sensors,
+                                const int32_t *anomaly, uint32_t window, uint32_t stride, uint32_t n_bins,
+                                uint32_t flags, double *edges_out, uint32_t *items_out, int32_t *labels_out,
+                                uint64_t *n_windows_out);
+
 /* ---------------------------------------------------------------- scoring */
 
 /* Load the frontier-scoring MLP used by SGFIM_ORDER_LEARNED: 3 layers,

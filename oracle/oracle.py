@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 __all__ = [
     "build", "lib", "build_bitmaps", "support_batch", "cooccurrence",
     "mine_mfi", "mine_fast", "mine_engine", "thresh_from", "tensorfim_mfis",
-    "anyfim_stages", "item_counts", "freq_order", "parse_fimi",
+    "anyfim_stages", "item_counts", "freq_order", "parse_fimi", "online_bins",
 ]
 
 
@@ -34,8 +34,9 @@ _lib = None
 
 def build(force=False):
     """Compile liboracle.so with gcc (the recipe lives in oracle/Makefile)."""
+    srcs = ("mfi_oracle.c", "online_oracle.c", "Makefile")
     if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "mfi_oracle.c")):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(os.path.join(HERE, s)) for s in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -53,6 +54,9 @@ def lib():
         L.orc_mine_fast.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_mine_engine.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint32, u32p, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_free.argtypes = [C.POINTER(_Mfis)]
+        L.orc_online_bins.argtypes = [C.POINTER(C.c_double), C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                      C.c_uint32, C.c_int, C.POINTER(C.c_double), u32p]
+        L.orc_online_bins.restype = C.c_int64
         for f in ("orc_mine_dfs", "orc_mine_fast", "orc_mine_engine"):
             getattr(L, f).restype = C.c_int
         _lib = L
@@ -174,6 +178,27 @@ def mine_engine(bm, thr, roots, node_cap=0):
 
 
 # ---------------------------------------------------------------- engine rules
+def online_bins(values, window=30, stride=15, n_bins=3, anomaly=None, n_threads=None):
+    """code/pipeline/online_discretize.py:22-128 (run_file over every sensor) in C
+    -> (edges [n_win, S, n_bins+1], items [n_win, S] sensor * n_bins + bin,
+    labels [n_win] = the window's max flag)."""
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    n, S = values.shape
+    n_win = (n - window) // stride + 1 if n >= window else 0
+    edges = np.zeros((max(n_win, 1), S, n_bins + 1), np.float64)
+    items = np.zeros((max(n_win, 1), S), np.uint32)
+    got = lib().orc_online_bins(_p(values, C.c_double), n, S, window, stride, n_bins,
+                                n_threads or os.cpu_count() or 1, _p(edges, C.c_double), _p(items, C.c_uint32))
+    if got < 0:
+        raise ValueError("orc_online_bins: bad arguments")
+    assert got == n_win
+    labels = np.zeros(n_win, np.int64)
+    if anomaly is not None:
+        for w in range(n_win):
+            labels[w] = int(np.max(anomaly[w * stride:w * stride + window]))
+    return edges[:n_win], items[:n_win].astype(np.int64), labels
+
+
 def parse_fimi(path):
     """kernel_bitmap.cu:205-233 byte scan: one transaction per '\\n' (empty lines
     kept as empty transactions), non-negative integers are items, a '-' and the

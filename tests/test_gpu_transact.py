@@ -71,3 +71,86 @@ def test_stream_to_windows_pipeline(engine):
             assert res.as_dict(w) == {frozenset(x): c for x, c in ref}, w
     finally:
         ring.close()
+
+
+# ---------------------------------------------------------------- online (P²) form
+
+ON_GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "online_golden.json")))["cases"]
+
+
+@pytest.mark.parametrize("case", ON_GOLD, ids=[f"seed{c['case']['seed']}" for c in ON_GOLD])
+def test_online_matches_reference(engine, case):
+    """sgfim_transactionize_online reproduces the reference run_file's items
+    and every window's P² edges bit for bit."""
+    import hashlib
+    c = case["case"]
+    vals, anom = datagen.sensor_stream(c["n_rows"], c["n_sensors"], c["seed"], constant_cols=c["constant_cols"])
+    items, labels, edges = engine.transactionize_online(vals, c["window"], c["stride"], c["n_bins"], anomaly=anom)
+    assert items.tolist() == case["items"]
+    head = case["edges_head"]
+    assert [[[float(x).hex() for x in e] for e in w] for w in edges[:len(head)]] == head
+    flat = np.ascontiguousarray(edges, dtype="<f8")
+    assert hashlib.sha256(flat.tobytes()).hexdigest() == case["edges_sha256"]
+    n_win = len(case["items"])
+    assert labels.tolist() == [int(anom[w * c["stride"]:w * c["stride"] + c["window"]].max()) for w in range(n_win)]
+
+
+@pytest.mark.parametrize("shape", [(200_000, 21, 30, 15, 3), (100_000, 16, 64, 8, 6), (50_000, 5, 5, 1, 2)])
+def test_online_large_matches_oracle(engine, shape):
+    """Long streams against the C restatement: edges of every window bit for
+    bit, items, labels; TX_LOAD makes the items the dataset."""
+    import oracle
+    n, S, window, stride, n_bins = shape
+    vals, anom = datagen.sensor_stream(n, S, 31 + S, constant_cols=(1,))
+    items, labels, edges = engine.transactionize_online(vals, window, stride, n_bins, anomaly=anom, load=True)
+    w_edges, w_items, w_labels = oracle.online_bins(vals, window, stride, n_bins, anom)
+    assert np.array_equal(edges.view(np.int64), w_edges.view(np.int64))
+    assert np.array_equal(items, w_items) and np.array_equal(labels, w_labels)
+    assert engine.info()["n_txn"] == len(items)
+    assert np.array_equal(engine.item_counts(S * n_bins), np.bincount(items.ravel(), minlength=S * n_bins))
+
+
+def test_online_edge_cases(engine):
+    vals, _ = datagen.sensor_stream(20, 2, 5)
+    items, labels, edges = engine.transactionize_online(vals, 30, 15, 3)     # no window fits
+    assert items.shape == (0, 2) and labels.shape == (0,) and edges.shape[0] == 0
+    items, labels, edges = engine.transactionize_online(np.zeros((0, 3)), 30, 15, 3)
+    assert items.shape == (0, 3)
+    const = np.full((500, 3), 2.5)                                            # zero spread: span = 1e-9
+    items, _, edges = engine.transactionize_online(const, 10, 5, 3)
+    w_edges, w_items, _ = __import__("oracle").online_bins(const, 10, 5, 3)
+    assert np.array_equal(edges.view(np.int64), w_edges.view(np.int64)) and np.array_equal(items, w_items)
+    bad = vals.copy()
+    bad[3, 1] = np.nan
+    with pytest.raises(SgfimError):
+        engine.transactionize_online(np.vstack([bad] * 5), 10, 5, 3)
+    for window, stride, n_bins in ((0, 1, 3), (5, 0, 3), (5, 1, 1), (5, 1, 65), (300, 1, 3)):
+        with pytest.raises(SgfimError):
+            engine.transactionize_online(np.ones((400, 2)), window, stride, n_bins)
+
+
+def test_online_run_file_and_report(engine):
+    """The reference-shaped host calls: run_file's [(win_idx, start, {col:
+    bin})] and the online-vs-offline agreement report, against the oracles."""
+    from oracle import online
+    from sgfim import online as son
+    cols = [f"s{i}" for i in range(8)]
+    frames = []
+    for seed in (40, 41, 42):
+        vals, _ = datagen.sensor_stream(3000 + 500 * (seed - 40), 8, seed)
+        frames.append({c: vals[:, i] for i, c in enumerate(cols)})
+    res = son.run_file(engine, frames[0], cols, 30, 15)
+    v0 = np.column_stack([frames[0][c] for c in cols])
+    _, want, _ = online.online_items(v0, 30, 15, 3)
+    assert [r[1] for r in res] == [15 * w for w in range(len(want))]
+    assert [[r[2][c] for c in cols] for r in res] == [[int(x) - 3 * i for i, x in enumerate(row)] for row in want]
+    report = son.online_vs_offline(engine, frames, cols, 30, 15)
+    seg = {k: [] for k in range(5)}
+    for f in frames:
+        v = np.column_stack([f[c] for c in cols])
+        _, on, _ = online.online_items(v, 30, 15, 3)
+        off, _ = transact.window_items(v, transact.fit_bins(v, 3), 30, 15, None, 3)
+        for w in range(len(on)):
+            seg[min(4, w * 5 // len(on))].append(float(np.count_nonzero(on[w] == off[w])) / 8)
+    assert report == {son.segment_key(i): {"files": 3, "windows": len(v), "item_agreement": round(float(np.mean(v)), 4)}
+                      for i, v in seg.items()}

@@ -185,3 +185,35 @@ def test_transact_oracle_matches_reference(case):
     assert [[float(x).hex() for x in e] for e in edges] == case["edges"]
     items, labels = transact.window_items(vals, edges, c["window"], c["stride"], anom, c["n_bins"])
     assert items.tolist() == case["items"] and labels.tolist() == case["labels"]
+
+
+ON_GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "online_golden.json")))["cases"]
+
+
+def _online_check(case, edges, items):
+    import hashlib
+    c = case["case"]
+    assert items.tolist() == case["items"]
+    assert [[[float(x).hex() for x in e] for e in w] for w in edges[:len(case["edges_head"])]] == case["edges_head"]
+    flat = np.ascontiguousarray(edges, dtype="<f8").reshape(len(case["items"]), c["n_sensors"], c["n_bins"] + 1)
+    assert hashlib.sha256(flat.tobytes()).hexdigest() == case["edges_sha256"]
+
+
+@pytest.mark.parametrize("case", ON_GOLD, ids=[f"seed{c['case']['seed']}" for c in ON_GOLD])
+def test_online_oracles_match_reference(case):
+    """Both restatements of the online discretiser (pure Python, and C in
+    liboracle.so) reproduce the reference run_file's items and every window's
+    edges bit for bit."""
+    import hashlib
+    from oracle import online, oracle
+    from sgfim import datagen
+    c = case["case"]
+    vals, anom = datagen.sensor_stream(c["n_rows"], c["n_sensors"], c["seed"], constant_cols=c["constant_cols"])
+    assert hashlib.sha256(np.ascontiguousarray(vals, dtype="<f8").tobytes()).hexdigest() == case["values_sha256"]
+    n_win = len(case["items"])
+    assert case["starts"] == [w * c["stride"] for w in range(n_win)]
+    e1, i1, l1 = online.online_items(vals, c["window"], c["stride"], c["n_bins"], anom)
+    _online_check(case, e1, i1)
+    e2, i2, l2 = oracle.online_bins(vals, c["window"], c["stride"], c["n_bins"], anom)
+    _online_check(case, e2, i2)
+    assert l1.tolist() == l2.tolist()

@@ -110,12 +110,12 @@ __global__ void quantile_kernel(const double *__restrict__ stats, uint32_t R, co
     edges[i] = v;
 }
 
-// numpy's median of `window` consecutive values (insertion sort while loading;
-// the mean of the two middle values for an even count).
-__device__ __forceinline__ double window_median(const double *__restrict__ col, uint32_t window) {
+// numpy's median of `window` values `step` elements apart (insertion sort while
+// loading; the mean of the two middle values for an even count).
+__device__ __forceinline__ double window_median(const double *__restrict__ col, uint32_t window, uint64_t step = 1) {
     double buf[kMaxWindow];
     for (uint32_t j = 0; j < window; ++j) {
-        const double v = col[j];
+        const double v = col[j * step];
         uint32_t k = j;
         while (k > 0 && buf[k - 1] > v) {
             buf[k] = buf[k - 1];
@@ -163,11 +163,31 @@ __global__ void window_bin_kernel(const double *__restrict__ cols, uint64_t n, u
 // feeds every row of every window, in window order, to every estimator (rows
 // shared by overlapping windows are fed again) and after each window bins the
 // window median with the edges of that moment (OnlineBinner.edges :87-103).
-// The estimator is a sequential recurrence, so the parallel axis is (sensor,
-// estimator); each one runs on lane 0 of its own warp, so that the warps spread
-// over the SMs' schedulers and every double operation of the chain issues at
-// once.  All arithmetic is explicitly rounded (no fused multiply-add), in the
-// reference's order, so the estimates are the reference's bit for bit.
+// An estimator is a sequential recurrence, so the parallel axis is the chain
+// (sensor, estimator).  A warp carries `lanes` chains (1..32): few chains run
+// one to a warp, so that every chain has a scheduler's double pipe to itself;
+// many chains share a warp.  All arithmetic is explicitly rounded (no fused
+// multiply-add), in the reference's order, so the estimates are the
+// reference's bit for bit.
+//
+// When the estimate stops changing.  The reference's value() is the middle
+// marker qv[2], and its marker rule can never move markers 2 and 3 for most
+// quantiles.  With gap_i = n[i+1] - n[i], the setup gives gaps (1+2q, 2q,
+// 2-2q, 1-2q); a sample in cell k adds 1 to every position and 1 more to
+// positions 1..k, so gap_0 grows by [k >= 1] and gap_i (i = 1..3) shrinks by
+// [k == i] -- gaps 1..3 never grow.  Marker i is tested only when d = gap_{i-1}
+// >= 1 and span = gap_{i-1} + gap_i > 1, and a move needs qv[i] + qp < qv[i+1]
+// with qp = (d+1) (qv[i+1] - qv[i-1]) / span >= (d+1)/span (qv[i+1] - qv[i]),
+// so it needs (d+1)/span < 1, i.e. gap_i > 1.  Marker 3 needs gap_3 = 1-2q > 1:
+// never.  Marker 2 needs gap_1 = 2q >= 1 and gap_2 = 2-2q > 1: never for
+// q != 1/2.  With q = j/n_bins and n_bins <= 64 both inequalities miss by at
+// least 1/64, far beyond the rounding of the positions and of qp.  So for q !=
+// 1/2 the estimate is fixed at the setup (the third smallest of the first five
+// samples).  For q = 1/2 the positions are integers and marker 2 can be tested
+// only while no sample fell in cell 1 or 2 (gap_1 = gap_2 = 1), or never when
+// qv[1] = qv[2] = qv[3] (qp = 0).  The kernel runs the recurrence until its
+// chain reaches such a state and then writes the fixed estimate for every
+// remaining window; `full` turns the shortcut off (the tests compare both).
 
 constexpr uint32_t kMaxOnlineBins = 64;
 
@@ -184,22 +204,37 @@ __device__ __forceinline__ void sort5(double (&a)[5]) {
             }
 }
 
-// est[(w * S + s) * m + j] = estimate j of sensor s after window w
-__global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t m,
+__global__ void nan_count_kernel(const double *__restrict__ v, uint64_t n, uint32_t *__restrict__ nan_count) {
+    uint32_t c = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        c += v[i] != v[i];
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(nan_count, c);
+}
+
+// est[(w * S + s) * m + j] = estimate j of sensor s after window w; chain c =
+// s * m + j reads rows[t * S + s] (row-major values: neighbouring lanes read
+// neighbouring sensors).
+__global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ rows, uint32_t S, uint32_t m,
                                                  const double *__restrict__ quant, uint32_t window, uint32_t stride,
-                                                 uint64_t n_win, double *__restrict__ est) {
-    const uint64_t e = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-    if ((threadIdx.x & 31) != 0 || e >= (uint64_t)S * m) return;
-    const uint32_t s = (uint32_t)(e / m), j = (uint32_t)(e - (uint64_t)s * m);
+                                                 uint64_t n_win, uint32_t lanes, uint32_t full,
+                                                 double *__restrict__ est) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t c = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * lanes + lane;
+    if (lane >= lanes || c >= (uint64_t)S * m) return;
+    const uint32_t s = (uint32_t)(c / m), j = (uint32_t)(c - (uint64_t)s * m);
     const double q = quant[j];
-    const double *col = cols + (uint64_t)s * n;
+    const bool half = q == 0.5;
+    const uint64_t chains = (uint64_t)S * m;
     double qv[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     double np_[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    uint32_t n_init = 0;
-    for (uint64_t w = 0; w < n_win; ++w) {
-        const uint64_t start = w * stride;
+    uint32_t n_init = 0;   // the same for every chain: all see the same rows
+    bool fixed = false;
+    uint64_t w = 0;
+    for (; w < n_win && !fixed; ++w) {
+        const double *x_ptr = rows + w * stride * S + s;
         for (uint32_t t = 0; t < window; ++t) {
-            const double x = col[start + t];
+            const double x = x_ptr[(uint64_t)t * S];
             if (n_init < 5) {
 #pragma unroll
                 for (int i = 0; i < 5; ++i)
@@ -211,6 +246,10 @@ __global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ cols
                     np_[2] = __dadd_rn(1.0, __dmul_rn(4.0, q));
                     np_[3] = __dadd_rn(3.0, __dmul_rn(2.0, q));
                     np_[4] = 4.0;
+                    if (!full && (!half || (qv[1] == qv[2] && qv[2] == qv[3]))) {
+                        fixed = true;
+                        break;
+                    }
                 }
                 continue;
             }
@@ -245,6 +284,11 @@ __global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ cols
                     if (qv[i - 1] < moved && moved < qv[i + 1]) qv[i] = moved;
                 }
             }
+            // q = 1/2: once a sample fell in cell 1 or 2, marker 2 is never tested again
+            if (!full && (k == 1 || k == 2)) {
+                fixed = true;
+                break;
+            }
         }
         double v;
         if (n_init >= 5) {
@@ -260,14 +304,16 @@ __global__ void __launch_bounds__(128) p2_kernel(const double *__restrict__ cols
             for (int i = 1; i < 5; ++i)
                 if ((uint32_t)i == n_init / 2) v = (n_init & 1) ? a[i] : __ddiv_rn(__dadd_rn(a[i - 1], a[i]), 2.0);
         }
-        est[(w * S + s) * m + j] = v;
+        est[w * chains + c] = v;
     }
+    // the estimate no longer changes: every remaining window gets it
+    for (; w < n_win; ++w) est[w * chains + c] = qv[2];
 }
 
 // One thread per (window, sensor): edges from the sensor's estimates after the
 // window, then the window median binned with them.
-__global__ void online_bin_kernel(const double *__restrict__ cols, uint64_t n, uint32_t S, uint32_t window,
-                                  uint32_t stride, uint64_t n_win, const double *__restrict__ est, uint32_t n_bins,
+__global__ void online_bin_kernel(const double *__restrict__ rows, uint32_t S, uint32_t window, uint32_t stride,
+                                  uint64_t n_win, const double *__restrict__ est, uint32_t n_bins,
                                   const int32_t *__restrict__ anomaly, double *__restrict__ edges,
                                   uint32_t *__restrict__ items, int32_t *__restrict__ labels) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -307,7 +353,7 @@ __global__ void online_bin_kernel(const double *__restrict__ cols, uint64_t n, u
     for (uint32_t j = 0; j < m; ++j) e[1 + j] = q[j];
     e[n_bins] = __dadd_rn(q[m - 1], span);
     const uint64_t start = w * stride;
-    const double med = window_median(cols + (uint64_t)s * n + start, window);
+    const double med = window_median(rows + start * S + s, window, S);
     uint32_t cnt = 0;   // edges <= med (searchsorted side="right")
     for (uint32_t j = 0; j <= n_bins; ++j) cnt += e[j] <= med;
     int32_t b = (int32_t)cnt - 1;
@@ -349,17 +395,16 @@ extern "C" int sgfim_transactionize_online(sgfim_handle *h, const double *values
     SG_CUDA_TRY(cudaSetDevice(h->device));
     cudaStream_t st = h->stream;
     const uint32_t S = n_sensors, m = n_bins - 1;
-    DevBuf d_rows, d_cols, d_est, d_out, d_anom;
+    DevBuf d_rows, d_est, d_out, d_anom;
     struct Free {
-        DevBuf *b[5];
+        DevBuf *b[4];
         ~Free() {
             for (DevBuf *x : b) x->release();
         }
-    } guard{{&d_rows, &d_cols, &d_est, &d_out, &d_anom}};
+    } guard{{&d_rows, &d_est, &d_out, &d_anom}};
     if (n_win) {
         const size_t mat = (size_t)n_rows * S * 8;
         d_rows.reserve(mat, st);
-        d_cols.reserve(mat, st);
         // out: nan count | quantiles | labels | items | edges
         size_t off = 0;
         auto carve = [&](size_t bytes) {
@@ -378,17 +423,25 @@ extern "C" int sgfim_transactionize_online(sgfim_handle *h, const double *values
         SG_CUDA_TRY(cudaMemsetAsync(base + o_nan, 0, 4, st));
         SG_CUDA_TRY(cudaMemcpyAsync(base + o_q, quant.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
         const uint64_t total = n_rows * S;
-        to_columns_kernel<<<(unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)h->n_sm * 32), 256, 0, st>>>(
-            d_rows.as<double>(), n_rows, S, d_cols.as<double>(), reinterpret_cast<uint32_t *>(base + o_nan));
+        nan_count_kernel<<<(unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)h->n_sm * 8), 256, 0, st>>>(
+            d_rows.as<double>(), total, reinterpret_cast<uint32_t *>(base + o_nan));
         SG_CUDA_TRY(cudaGetLastError());
         uint32_t nan_count = 0;
         SG_CUDA_TRY(cudaMemcpyAsync(&nan_count, base + o_nan, 4, cudaMemcpyDeviceToHost, st));
         SG_CUDA_TRY(cudaStreamSynchronize(st));
         if (nan_count) return fail(h, SGFIM_EINVAL, "the stream holds NaN values");
-        const uint64_t n_est = (uint64_t)S * m;
-        p2_kernel<<<(unsigned)((n_est + 3) / 4), 128, 0, st>>>(d_cols.as<double>(), n_rows, S, m,
+        // chains per warp: one while there are fewer chains than schedulers, then
+        // as many as it takes to keep the warp count at about one per scheduler
+        const uint64_t chains = (uint64_t)S * m;
+        const uint64_t sched = (uint64_t)h->n_sm * 4;
+        uint32_t lanes = (flags >> 8) & 63u;
+        if (lanes == 0) lanes = (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(1, (chains + sched - 1) / sched));
+        if (lanes > 32) return fail(h, SGFIM_EINVAL, "more than 32 chains per warp");
+        const uint64_t warps = (chains + lanes - 1) / lanes;
+        p2_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(d_rows.as<double>(), S, m,
                                                               reinterpret_cast<const double *>(base + o_q), window,
-                                                              stride, n_win, d_est.as<double>());
+                                                              stride, n_win, lanes, (flags & SGFIM_TX_P2_FULL) ? 1u : 0u,
+                                                              d_est.as<double>());
         SG_CUDA_TRY(cudaGetLastError());
         if (anomaly) {
             d_anom.reserve(n_rows * 4, st);
@@ -396,7 +449,7 @@ extern "C" int sgfim_transactionize_online(sgfim_handle *h, const double *values
         }
         const uint64_t nt = n_win * S;
         online_bin_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(
-            d_cols.as<double>(), n_rows, S, window, stride, n_win, d_est.as<double>(), n_bins,
+            d_rows.as<double>(), S, window, stride, n_win, d_est.as<double>(), n_bins,
             anomaly ? d_anom.as<int32_t>() : nullptr, reinterpret_cast<double *>(base + o_edges),
             reinterpret_cast<uint32_t *>(base + o_items), reinterpret_cast<int32_t *>(base + o_lab));
         SG_CUDA_TRY(cudaGetLastError());

@@ -170,10 +170,13 @@ class Engine:
         return items[:n_win * S].reshape(n_win, S).astype(np.int64), labels[:n_win].astype(np.int64), e
 
     def transactionize_online(self, values, window=30, stride=15, n_bins=3, anomaly=None, load=False,
-                              with_edges=True):
+                              with_edges=True, lanes=0, full_recurrence=False):
         """Online form (P² edges per window, sgfim_transactionize_online):
         -> (items [n_windows, n_sensors] dense ids, labels [n_windows], edges
-        [n_windows, n_sensors, n_bins+1] or None without ``with_edges``)."""
+        [n_windows, n_sensors, n_bins+1] or None without ``with_edges``).
+        ``lanes``: estimator chains per warp (0 = automatic);
+        ``full_recurrence``: step every estimator through the whole stream
+        instead of stopping once its estimate can no longer change."""
         values = np.ascontiguousarray(values, dtype=np.float64)
         if values.ndim != 2:
             raise ValueError("values must be [n_rows, n_sensors]")
@@ -191,7 +194,9 @@ class Engine:
         rc = self._L.sgfim_transactionize_online(
             self._h, _p(values, C.c_double), n, S,
             an.ctypes.data_as(C.POINTER(C.c_int32)) if an is not None else None, window, stride, n_bins,
-            L.TX_LOAD if load else 0, _p(edges, C.c_double) if with_edges else None, _p(items, C.c_uint32),
+            (L.TX_LOAD if load else 0) | (L.TX_P2_FULL if full_recurrence else 0) | ((int(lanes) & 63) << 8),
+            _p(edges, C.c_double) if with_edges else None,
+            _p(items, C.c_uint32),
             labels.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(nw))
         self._check(rc)
         assert nw.value == n_win

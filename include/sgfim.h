@@ -397,7 +397,16 @@ int sgfim_transactionize(sgfim_handle *h, const double *values, uint64_t n_rows,
  * items_out[w * n_sensors + s] = s * n_bins + bin, labels_out[w] as in
  * sgfim_transactionize.  Windows as in sgfim_transactionize; a stream shorter
  * than one window gives 0 windows and SGFIM_OK.  2 <= n_bins <= 64, window <=
- * 256, NaN-free values (EINVAL otherwise).  SGFIM_TX_LOAD as above. */
+ * 256, NaN-free values (EINVAL otherwise).  SGFIM_TX_LOAD as above.  Each
+ * (sensor, estimator) is one sequential chain; SGFIM_TX_LANES(l) packs l
+ * chains (1..32) into a warp, 0 (the default) picks one chain per warp until
+ * the warps outnumber the SMs' schedulers.  The reference's marker rule never
+ * moves the middle marker for q != 1/2 (and for q = 1/2 only until a sample
+ * falls between markers 1 and 3), so a chain stops stepping once its estimate
+ * can no longer change; SGFIM_TX_P2_FULL runs every step instead (same
+ * results). */
+#define SGFIM_TX_LANES(l) (((uint32_t)(l) & 63u) << 8)
+#define SGFIM_TX_P2_FULL 0x2u
 int sgfim_transactionize_online(sgfim_handle *h, const double *values, uint64_t n_rows, uint32_t n_sensors,
                                 const int32_t *anomaly, uint32_t window, uint32_t stride, uint32_t n_bins,
                                 uint32_t flags, double *edges_out, uint32_t *items_out, int32_t *labels_out,

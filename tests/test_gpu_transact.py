@@ -78,14 +78,16 @@ def test_stream_to_windows_pipeline(engine):
 ON_GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "online_golden.json")))["cases"]
 
 
+@pytest.mark.parametrize("full", [False, True], ids=["fixed-estimate-exit", "full-recurrence"])
 @pytest.mark.parametrize("case", ON_GOLD, ids=[f"seed{c['case']['seed']}" for c in ON_GOLD])
-def test_online_matches_reference(engine, case):
+def test_online_matches_reference(engine, case, full):
     """sgfim_transactionize_online reproduces the reference run_file's items
-    and every window's P² edges bit for bit."""
+    and every window's P² edges bit for bit, with and without the early exit."""
     import hashlib
     c = case["case"]
     vals, anom = datagen.sensor_stream(c["n_rows"], c["n_sensors"], c["seed"], constant_cols=c["constant_cols"])
-    items, labels, edges = engine.transactionize_online(vals, c["window"], c["stride"], c["n_bins"], anomaly=anom)
+    items, labels, edges = engine.transactionize_online(vals, c["window"], c["stride"], c["n_bins"], anomaly=anom,
+                                                        full_recurrence=full)
     assert items.tolist() == case["items"]
     head = case["edges_head"]
     assert [[[float(x).hex() for x in e] for e in w] for w in edges[:len(head)]] == head
@@ -95,14 +97,16 @@ def test_online_matches_reference(engine, case):
     assert labels.tolist() == [int(anom[w * c["stride"]:w * c["stride"] + c["window"]].max()) for w in range(n_win)]
 
 
+@pytest.mark.parametrize("full", [False, True], ids=["fixed-estimate-exit", "full-recurrence"])
 @pytest.mark.parametrize("shape", [(200_000, 21, 30, 15, 3), (100_000, 16, 64, 8, 6), (50_000, 5, 5, 1, 2)])
-def test_online_large_matches_oracle(engine, shape):
+def test_online_large_matches_oracle(engine, shape, full):
     """Long streams against the C restatement: edges of every window bit for
     bit, items, labels; TX_LOAD makes the items the dataset."""
     import oracle
     n, S, window, stride, n_bins = shape
     vals, anom = datagen.sensor_stream(n, S, 31 + S, constant_cols=(1,))
-    items, labels, edges = engine.transactionize_online(vals, window, stride, n_bins, anomaly=anom, load=True)
+    items, labels, edges = engine.transactionize_online(vals, window, stride, n_bins, anomaly=anom, load=True,
+                                                        full_recurrence=full)
     w_edges, w_items, w_labels = oracle.online_bins(vals, window, stride, n_bins, anom)
     assert np.array_equal(edges.view(np.int64), w_edges.view(np.int64))
     assert np.array_equal(items, w_items) and np.array_equal(labels, w_labels)
@@ -154,3 +158,44 @@ def test_online_run_file_and_report(engine):
             seg[min(4, w * 5 // len(on))].append(float(np.count_nonzero(on[w] == off[w])) / 8)
     assert report == {son.segment_key(i): {"files": 3, "windows": len(v), "item_agreement": round(float(np.mean(v)), 4)}
                       for i, v in seg.items()}
+
+
+@pytest.mark.parametrize("lanes", [1, 3, 32, 0])
+def test_online_chain_packing(engine, lanes):
+    """Any number of estimator chains per warp gives the same bits: 300
+    sensors x 4 estimators = 1,200 chains, partial last warp (full recurrence,
+    so that every chain steps through the whole stream)."""
+    import oracle
+    vals, anom = datagen.sensor_stream(3_000, 300, 77, constant_cols=(0, 299))
+    items, labels, edges = engine.transactionize_online(vals, 20, 7, 5, anomaly=anom, lanes=lanes,
+                                                        full_recurrence=True)
+    w_edges, w_items, w_labels = oracle.online_bins(vals, 20, 7, 5, anom)
+    assert np.array_equal(edges.view(np.int64), w_edges.view(np.int64))
+    assert np.array_equal(items, w_items) and np.array_equal(labels, w_labels)
+
+
+@pytest.mark.parametrize("n_bins", [2, 4, 6])
+def test_online_half_quantile_streams(engine, n_bins):
+    """The estimator at q = 1/2 keeps stepping while no sample has fallen
+    between its markers 1 and 3: streams that stay in the outer cells for a
+    long stretch (and ones whose first samples tie) against the C restatement."""
+    import oracle
+    rng = np.random.default_rng(n_bins)
+    cols = []
+    # distinct first samples, then a long run in the outer cells, then noise
+    head = [0.0, 1.0, 2.0, 3.0, 5.0]
+    outer = np.where(np.arange(4000) % 2 == 0, 10.0, -10.0)
+    cols.append(np.concatenate([head, outer, rng.normal(2.0, 2.0, 2000)]))
+    # tied first samples (markers 1..3 equal), then outer run
+    cols.append(np.concatenate([[0.0, 1.0, 1.0, 1.0, 5.0], outer, rng.normal(1.0, 1.0, 2000)]))
+    # markers 1 and 2 tied, 3 above
+    cols.append(np.concatenate([[0.0, 1.0, 1.0, 4.0, 5.0], outer, rng.normal(3.0, 1.0, 2000)]))
+    # ordinary noise
+    cols.append(rng.normal(0.0, 1.0, 6005))
+    vals = np.column_stack(cols)
+    for window, stride in ((30, 15), (3, 2), (7, 7)):
+        for full in (False, True):
+            items, _, edges = engine.transactionize_online(vals, window, stride, n_bins, full_recurrence=full)
+            w_edges, w_items, _ = oracle.online_bins(vals, window, stride, n_bins)
+            assert np.array_equal(edges.view(np.int64), w_edges.view(np.int64)), (window, stride, full)
+            assert np.array_equal(items, w_items)

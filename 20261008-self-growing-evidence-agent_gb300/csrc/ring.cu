@@ -35,6 +35,14 @@ struct sgfim_ring {
     std::string err;
 };
 
+// CTAs per SM of the cross-subtree filter (each holds one window's candidate
+// rows in its own scratch).  On the 4,096 service windows, largest first: 2 per
+// SM 59 ms, 4 per SM 46.5 ms, 8 per SM 45.4 ms.
+#ifndef SGFIM_WFILTER_CTAS_PER_SM
+#define SGFIM_WFILTER_CTAS_PER_SM 8
+#endif
+constexpr uint64_t kFilterCtasPerSm = SGFIM_WFILTER_CTAS_PER_SM;
+
 namespace sg {
 
 // Clear ring bits [p0, p0 + n) (positions modulo the ring size) in every row.
@@ -636,27 +644,39 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                     nodes[t_win[t]] += nodes_h[t];
                     if (st_h[t] != 0) bad[t_win[t]] = 1;
                 }
-                // ---- 5. cross-subtree filter of the split windows whose tasks all succeeded
-                std::vector<uint32_t> fwin, task0, task_of;
-                std::vector<uint64_t> first, wtotal;
+                // ---- 5. cross-subtree filter of the split windows whose tasks all succeeded,
+                // largest candidate sets first (a CTA per window; the big ones set the makespan)
+                struct FWin {
+                    uint32_t w;
+                    uint64_t t_lo, t_hi, m;
+                };
+                std::vector<FWin> fw;
                 uint64_t max_m = 0;
                 for (uint64_t t = 0; t < nt;) {
                     const uint32_t w = t_win[t];
                     uint64_t t2 = t;
                     while (t2 < nt && t_win[t2] == w) ++t2;
                     if (is_split[w] && !bad[w]) {
-                        task0.push_back((uint32_t)task_of.size());
                         uint64_t m = 0;
-                        for (uint64_t x = t; x < t2; ++x) {
-                            task_of.push_back((uint32_t)x);   // tasks were created in depth-first order
-                            first.push_back(m);
-                            m += cnt_h[x];
-                        }
-                        fwin.push_back(w);
-                        wtotal.push_back(m);
+                        for (uint64_t x = t; x < t2; ++x) m += cnt_h[x];
+                        fw.push_back({w, t, t2, m});
                         max_m = std::max(max_m, m);
                     }
                     t = t2;
+                }
+                std::stable_sort(fw.begin(), fw.end(), [](const FWin &a, const FWin &b) { return a.m > b.m; });
+                std::vector<uint32_t> fwin, task0, task_of;
+                std::vector<uint64_t> first, wtotal;
+                for (const FWin &f : fw) {
+                    task0.push_back((uint32_t)task_of.size());
+                    uint64_t m = 0;
+                    for (uint64_t x = f.t_lo; x < f.t_hi; ++x) {
+                        task_of.push_back((uint32_t)x);   // tasks were created in depth-first order
+                        first.push_back(m);
+                        m += cnt_h[x];
+                    }
+                    fwin.push_back(f.w);
+                    wtotal.push_back(m);
                 }
                 task0.push_back((uint32_t)task_of.size());
                 kept.assign(cnt_h.begin(), cnt_h.end());
@@ -668,7 +688,9 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                     SG_CUDA_TRY(cudaMemcpyAsync(dt_kept, dt_cnt, nt * 4, cudaMemcpyDeviceToDevice, st));
                     const uint64_t W = (max_m + 63) / 64;
                     const uint64_t scratch_words = std::max<uint64_t>(W * r->d, 64);
-                    const uint64_t ctas = std::min<uint64_t>(fwin.size(), (uint64_t)h->n_sm * 2);
+                    const uint64_t ctas = std::min<uint64_t>(
+                        fwin.size(), std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)h->n_sm * kFilterCtasPerSm,
+                                                                              (h->hbm_budget / 8) / (scratch_words * 8))));
                     // tables: first u64 | total u64 | task0 u32 | task_of u32 | status i32, then the scratch
                     const size_t tab =
                         ((first.size() + wtotal.size()) * 8 + (task0.size() + task_of.size() + fwin.size()) * 4 + 255) &

@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 __all__ = [
     "build", "lib", "build_bitmaps", "support_batch", "cooccurrence",
     "mine_mfi", "mine_fast", "mine_engine", "thresh_from", "tensorfim_mfis",
-    "anyfim_stages", "item_counts", "freq_order", "parse_fimi", "online_bins",
+    "anyfim_stages", "item_counts", "freq_order", "parse_fimi", "online_bins", "planted_kat",
+    "bmma_bench_bits",
 ]
 
 
@@ -34,7 +35,7 @@ _lib = None
 
 def build(force=False):
     """Compile liboracle.so with gcc (the recipe lives in oracle/Makefile)."""
-    srcs = ("mfi_oracle.c", "online_oracle.c", "Makefile")
+    srcs = ("mfi_oracle.c", "online_oracle.c", "kat_oracle.c", "Makefile")
     if force or not os.path.exists(LIB_PATH) or \
             os.path.getmtime(LIB_PATH) < max(os.path.getmtime(os.path.join(HERE, s)) for s in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -57,6 +58,9 @@ def lib():
         L.orc_online_bins.argtypes = [C.POINTER(C.c_double), C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                       C.c_uint32, C.c_int, C.POINTER(C.c_double), u32p]
         L.orc_online_bins.restype = C.c_int64
+        L.orc_planted_kat.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, u32p, u32p, u32p,
+                                      C.POINTER(C.c_double)]
+        L.orc_planted_kat.restype = C.c_int
         for f in ("orc_mine_dfs", "orc_mine_fast", "orc_mine_engine"):
             getattr(L, f).restype = C.c_int
         _lib = L
@@ -197,6 +201,42 @@ def online_bins(values, window=30, stride=15, n_bins=3, anomaly=None, n_threads=
         for w in range(n_win):
             labels[w] = int(np.max(anomaly[w * stride:w * stride + window]))
     return edges[:n_win], items[:n_win].astype(np.int64), labels
+
+
+def bmma_bench_bits(words, seed):
+    """bmma_bench.cu:196-207 fill_random_bits restated: two xorshift streams
+    ANDed, folded with the upper half (~12.5% density) -> (uint32 words, state)."""
+    m = (1 << 64) - 1
+    s = seed
+    s2 = (seed * 0x2545F4914F6CDD1D + 0x123456789) & m
+    out = np.empty(words, dtype=np.uint32)
+    for w in range(words):
+        s ^= (s << 13) & m
+        s ^= s >> 7
+        s ^= (s << 17) & m
+        s2 ^= (s2 << 13) & m
+        s2 ^= s2 >> 7
+        s2 ^= (s2 << 17) & m
+        out[w] = (s & s2 & 0xFFFFFFFF) & (s >> 32)
+    return out, s
+
+
+def planted_kat(n_tx=1 << 23, d=512, n_pat=80, maxpat=6):
+    """batch_proto.cu:45-51,193-231: the reference's planted-pattern data set
+    -> (bitmaps uint64 [d, n_tx/64], patterns [tuple of items], frequencies,
+    minsup = (int)(n_tx * 0.15 / 100))."""
+    W32 = n_tx // 32
+    bits = np.zeros(d * W32, dtype=np.uint32)
+    ptr = np.zeros(n_pat + 1, dtype=np.uint32)
+    items = np.zeros(n_pat * maxpat, dtype=np.uint32)
+    freq = np.zeros(n_pat, dtype=np.float64)
+    rc = lib().orc_planted_kat(n_tx, d, n_pat, maxpat, _p(bits, C.c_uint32), _p(ptr, C.c_uint32),
+                               _p(items, C.c_uint32), _p(freq, C.c_double))
+    if rc != 0:
+        raise ValueError("orc_planted_kat: bad arguments")
+    pats = [tuple(int(x) for x in items[ptr[p]:ptr[p + 1]]) for p in range(n_pat)]
+    bm = bits.view(np.uint64).reshape(d, W32 // 2)
+    return bm, pats, freq, int(n_tx * 0.15 / 100.0)
 
 
 def parse_fimi(path):

@@ -79,25 +79,11 @@ def test_node_cap_raises_like_reference():
 
 
 # ------------------------------------------------------------------ counting KATs
-def xorshift_bits(words, seed):
-    """bmma_bench.cu:196-207 fill_random_bits restated: two xorshift streams
-    ANDed, folded with the upper half (~12.5% density)."""
-    m = (1 << 64) - 1
-    s = seed
-    s2 = (seed * 0x2545F4914F6CDD1D + 0x123456789) & m
-    out = np.empty(words, dtype=np.uint32)
-    for w in range(words):
-        s ^= (s << 13) & m; s ^= s >> 7; s ^= (s << 17) & m
-        s2 ^= (s2 << 13) & m; s2 ^= s2 >> 7; s2 ^= (s2 << 17) & m
-        out[w] = (s & s2 & 0xFFFFFFFF) & (s >> 32)
-    return out, s
-
-
 def test_support_and_cooccurrence_kat():
     # bmma_bench's correctness gate shape scaled down: N bits, d items, sparse seeded bits
     N, d = 4096, 24
     w32 = N // 32
-    bits, _ = xorshift_bits(w32 * d, 0x9E3779B97F4A7C15)
+    bits, _ = oracle.bmma_bench_bits(w32 * d, 0x9E3779B97F4A7C15)
     bm32 = bits.reshape(d, w32)
     bm = bm32.view(np.uint64).reshape(d, w32 // 2)
     dense = np.unpackbits(bm32.view(np.uint8), axis=1, bitorder="little").astype(np.int64)
@@ -217,3 +203,16 @@ def test_online_oracles_match_reference(case):
     e2, i2, l2 = oracle.online_bins(vals, c["window"], c["stride"], c["n_bins"], anom)
     _online_check(case, e2, i2)
     assert l1.tolist() == l2.tolist()
+
+
+def test_planted_kat_generator_small():
+    """batch_proto.cu:195-231 restated: patterns of 2..6 distinct sorted items,
+    frequencies in [0.2%, 1.5%], every pattern's support near its frequency."""
+    bm, pats, freq, minsup = oracle.planted_kat(1 << 18)
+    assert bm.shape == (512, (1 << 18) // 64) and len(pats) == 80 and minsup == int((1 << 18) * 0.15 / 100.0)
+    assert all(2 <= len(p) <= 6 and list(p) == sorted(set(p)) for p in pats)
+    assert ((freq >= 0.002) & (freq <= 0.015)).all()
+    cp = np.cumsum([0] + [len(p) for p in pats]).astype(np.uint64)
+    ci = np.array([x for p in pats for x in p], np.uint32)
+    sup = oracle.support_batch(bm, cp, ci)
+    assert (sup >= (freq * (1 << 18) * 0.7).astype(np.int64)).all()

@@ -276,6 +276,7 @@ int sgfim_load_bitmaps(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uin
     Dataset &ds = h->ds;
     reset_dataset(ds);
     ds.source = "<bitmaps>";
+    ds.remap_identity = true;
     ds.n_txn = n_txn;
     ds.n_ids = d;
     ds.d = d;
@@ -376,30 +377,35 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
     if (!h || (n_cand && (!cand_ptr || !out))) return fail(h, SGFIM_EINVAL, "null argument");
     if (!h->ds.loaded) return fail(h, SGFIM_ESTATE, "no dataset loaded");
     if (n_cand && cand_ptr[0] != 0) return fail(h, SGFIM_EINVAL, "cand_ptr[0] must be 0");
-    for (uint64_t c = 0; c < n_cand; ++c)
-        if (cand_ptr[c + 1] < cand_ptr[c]) return fail(h, SGFIM_EINVAL, "cand_ptr must be non-decreasing");
     API_GUARD_BEGIN
     cudaSetDevice(h->device);
     Dataset &ds = h->ds;
     const uint64_t n_items = n_cand ? cand_ptr[n_cand] : 0;
     if (n_cand == 0) return SGFIM_OK;
-    // original ids -> dense rows; ids that never occur map past the last row (support 0)
-    std::vector<uint32_t> dense(n_items);
-    for (uint64_t j = 0; j < n_items; ++j) {
-        const uint32_t id = cand_items[j];
-        dense[j] = (id < ds.n_ids && ds.o2d[id] >= 0) ? (uint32_t)ds.o2d[id] : 0xfffffffeu;
-    }
     if (ds.d == 0 || ds.n_txn == 0) {
+        for (uint64_t c = 0; c < n_cand; ++c)
+            if (cand_ptr[c + 1] < cand_ptr[c]) return fail(h, SGFIM_EINVAL, "cand_ptr must be non-decreasing");
         for (uint64_t c = 0; c < n_cand; ++c) out[c] = cand_ptr[c + 1] == cand_ptr[c] ? (uint32_t)ds.n_txn : 0;
         return SGFIM_OK;
     }
-    h->cand_ptr_dev.reserve((n_cand + 1) * 8, h->stream);
+    // the CSR goes to the device as given; the monotonicity check and the original id ->
+    // dense row mapping (ids that never occur map past the last row: support 0) run there
+    h->cand_ptr_dev.reserve((n_cand + 1) * 8 + 8, h->stream);
     h->cand_items_dev.reserve(std::max<uint64_t>(n_items, 1) * 4, h->stream);
     h->out_dev.reserve(n_cand * 4, h->stream);
+    uint32_t *d_bad = reinterpret_cast<uint32_t *>(h->cand_ptr_dev.as<uint64_t>() + n_cand + 1);
     SG_CUDA_TRY(cudaMemcpyAsync(h->cand_ptr_dev.ptr, cand_ptr, (n_cand + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+    SG_CUDA_TRY(cudaMemsetAsync(d_bad, 0, 4, h->stream));
     if (n_items)
-        SG_CUDA_TRY(cudaMemcpyAsync(h->cand_items_dev.ptr, dense.data(), n_items * 4, cudaMemcpyHostToDevice,
+        SG_CUDA_TRY(cudaMemcpyAsync(h->cand_items_dev.ptr, cand_items, n_items * 4, cudaMemcpyHostToDevice,
                                     h->stream));
+    launch_cand_prep(h->cand_ptr_dev.as<uint64_t>(), n_cand, h->cand_items_dev.as<uint32_t>(), n_items,
+                     ds.remap_identity ? nullptr : ds.remap.as<int32_t>(), ds.n_ids, d_bad, h->stream, h->n_sm);
+    ++h->launches;
+    uint32_t bad_h = 0;
+    SG_CUDA_TRY(cudaMemcpyAsync(&bad_h, d_bad, 4, cudaMemcpyDeviceToHost, h->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (bad_h) return fail(h, SGFIM_EINVAL, "cand_ptr must be non-decreasing");
     h->support_scratch.reserve(support_scratch_bytes(n_cand), h->stream);
     SupportScratch sc{h->support_scratch.ptr, h->support_scratch.bytes};
     const SupportPlan &plan = h->plan;

@@ -51,6 +51,7 @@ struct Dataset {
     uint64_t stride = 0;         // words per row (even)
     DevBuf bitmaps;
     DevBuf remap;                // int32 o2d on device (load_fimi/csr path)
+    bool remap_identity = false; // bitmap loads: row = original id, remap unused
     DevBuf sup_dev;
     CUtensorMap map{};
     bool map_ok = false;

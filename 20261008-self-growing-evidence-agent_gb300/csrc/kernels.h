@@ -42,6 +42,9 @@ struct QueryBatch {
 void launch_transpose(const uint64_t *row_ptr, const uint32_t *items, uint64_t n_txn, const int32_t *remap,
                       uint32_t d, uint64_t *bitmaps, uint64_t stride, uint32_t *counts, cudaStream_t st,
                       int n_sm);
+// host candidate CSR on the device: monotonicity check (bad |= 1) and id -> row mapping in place
+void launch_cand_prep(const uint64_t *cand_ptr, uint64_t n_cand, uint32_t *items, uint64_t n_items,
+                      const int32_t *remap, uint32_t n_ids, uint32_t *bad, cudaStream_t st, int n_sm);
 void launch_row_popc(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t *counts,
                      cudaStream_t st);
 void launch_queries(const QueryBatch &qb, cudaStream_t st, int n_sm);

@@ -127,6 +127,37 @@ void launch_transpose(const uint64_t *row_ptr, const uint32_t *items, uint64_t n
     SG_CUDA_TRY(cudaGetLastError());
 }
 
+namespace {
+// Candidate CSR from the host, checked and mapped on the device: bad[0] |= 1 when
+// cand_ptr decreases anywhere; items become dense rows (ids that never occur map
+// past the last row, where every support is 0).  remap null = identity on [0, n_ids).
+__global__ void cand_prep_kernel(const uint64_t *__restrict__ cand_ptr, uint64_t n_cand, uint32_t *__restrict__ items,
+                                 uint64_t n_items, const int32_t *__restrict__ remap, uint32_t n_ids,
+                                 uint32_t *__restrict__ bad) {
+    const uint64_t n = n_cand > n_items ? n_cand : n_items;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < n_cand && cand_ptr[i + 1] < cand_ptr[i]) atomicOr(bad, 1u);
+        if (i < n_items) {
+            const uint32_t id = items[i];
+            uint32_t r = 0xfffffffeu;
+            if (id < n_ids) {
+                const int32_t m = remap ? remap[id] : (int32_t)id;
+                if (m >= 0) r = (uint32_t)m;
+            }
+            items[i] = r;
+        }
+    }
+}
+}  // namespace
+
+void launch_cand_prep(const uint64_t *cand_ptr, uint64_t n_cand, uint32_t *items, uint64_t n_items,
+                      const int32_t *remap, uint32_t n_ids, uint32_t *bad, cudaStream_t st, int n_sm) {
+    const uint64_t n = std::max<uint64_t>(std::max(n_cand, n_items), 1);
+    const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)n_sm * 8);
+    cand_prep_kernel<<<blocks, 256, 0, st>>>(cand_ptr, n_cand, items, n_items, remap, n_ids, bad);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
 void launch_row_popc(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t d, uint32_t *counts,
                      cudaStream_t st) {
     if (d == 0) return;

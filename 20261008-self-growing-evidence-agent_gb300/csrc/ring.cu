@@ -230,6 +230,7 @@ int sgfim_ring_window_load(sgfim_ring *r, sgfim_handle *h, uint64_t start, uint6
         Dataset &ds = h->ds;
         reset_dataset(ds);
         ds.source = "<ring window>";
+        ds.remap_identity = true;
         ds.n_txn = len;
         ds.n_ids = r->d;
         ds.d = r->d;

@@ -222,13 +222,19 @@ class Engine:
         return out[:n]
 
     # ------------------------------------------------------------ counting
-    def support_batch(self, cand_ptr, cand_items):
+    def support_batch(self, cand_ptr, cand_items, out=None):
+        """Supports of the CSR candidates (original ids).  ``out``: an optional
+        uint32 array of at least n_cand entries to write into (e.g. pinned host
+        memory, so that the device-to-host copy runs at full speed)."""
         cand_ptr = np.ascontiguousarray(cand_ptr, dtype=np.uint64)
         cand_items = np.ascontiguousarray(cand_items, dtype=np.uint32)
         if len(cand_items) == 0:
             cand_items = np.zeros(1, np.uint32)
         n = len(cand_ptr) - 1
-        out = np.zeros(max(n, 1), dtype=np.uint32)
+        if out is None:
+            out = np.zeros(max(n, 1), dtype=np.uint32)
+        elif out.dtype != np.uint32 or not out.flags.c_contiguous or len(out) < max(n, 1):
+            raise ValueError("out must be a contiguous uint32 array of n_cand entries")
         self._check(self._L.sgfim_support_batch(self._h, _p(cand_ptr, C.c_uint64), _p(cand_items, C.c_uint32),
                                                 n, _p(out, C.c_uint32)))
         return out[:n]

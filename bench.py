@@ -332,12 +332,13 @@ def main():
         pin_bm = torch.from_numpy(bm.view(np.int64)).pin_memory().numpy().view(np.uint64)
         pin_cp = torch.from_numpy(cp.view(np.int64)).pin_memory().numpy().view(np.uint64)
         pin_ci = torch.from_numpy(ci.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        pin_out = torch.zeros(n_cand, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
         host = Engine(device=local)
         e_times = []
         for s in range(1 + args.e2e_steps):
             t0 = time.perf_counter()
             host.load_bitmaps(pin_bm, WORKLOAD["n_txn"])
-            sup = host.support_batch(pin_cp, pin_ci)
+            sup = host.support_batch(pin_cp, pin_ci, out=pin_out)
             dt = time.perf_counter() - t0
             if s > 0:
                 e_times.append(dt)

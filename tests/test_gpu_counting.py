@@ -72,6 +72,28 @@ def test_support_batch_edge_candidates(engine):
         assert got[i] == want, (i, s)
 
 
+def test_support_batch_bad_csr_and_sparse_ids(engine):
+    """A decreasing cand_ptr is refused (checked on the device) and the handle
+    stays usable; after a CSR load (sparse original ids) candidates map through
+    the device remap: absent ids give 0."""
+    from sgfim.engine import SgfimError
+    bm = _bitmaps(4096, 20, seed=4)
+    engine.load_bitmaps(bm, 4096)
+    with pytest.raises(SgfimError):
+        engine.support_batch(np.array([0, 3, 2, 4], np.uint64), np.array([1, 2, 3, 4], np.uint32))
+    assert engine.support_batch(np.array([0, 1], np.uint64), np.array([3], np.uint32))[0] == \
+        oracle.support_batch(bm, np.array([0, 1], np.uint64), np.array([3], np.uint32))[0]
+    rows = [[5, 100, 7], [100, 7], [5], [900, 5, 7], [7]]
+    rp, it = datagen.txns_to_csr(rows)
+    engine.load_csr(rp, it)
+    sets = [[5], [7, 100], [5, 7], [900], [6], [1000], [5, 7, 900], []]
+    cp = np.zeros(len(sets) + 1, np.uint64)
+    cp[1:] = np.cumsum([len(x) for x in sets])
+    ci = np.array([x for x in sets for x in x], np.uint32)
+    want = [sum(1 for r in rows if set(x) <= set(r)) for x in sets]
+    assert engine.support_batch(cp, ci).tolist() == want
+
+
 def test_support_batch_device_pointer_api(engine):
     torch = pytest.importorskip("torch")
     n_txn, d = 32 * 1024, 128

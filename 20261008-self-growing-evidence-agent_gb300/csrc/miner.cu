@@ -31,6 +31,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 #include "common.cuh"
 #include "engine.h"
@@ -68,6 +69,21 @@ struct QuerySet {
     }
 };
 
+// Runs fn(lo, hi) over [0, n) split into contiguous ranges on the host's cores
+// (the result assembly after the search; each range writes only its own slice).
+template <class F> void parallel_ranges(uint64_t n, F &&fn) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t t = std::min<uint64_t>(std::min<uint64_t>(hw, 32), std::max<uint64_t>(1, n / 4096));
+    if (t <= 1) {
+        fn((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(t);
+    for (uint64_t i = 0; i < t; ++i) th.emplace_back([&, i] { fn(n * i / t, n * (i + 1) / t); });
+    for (auto &x : th) x.join();
+}
+
 class Miner {
   public:
     Miner(sgfim_handle *h, const sgfim_mine_params &p)
@@ -97,6 +113,7 @@ class Miner {
     // candidates (host)
     std::vector<uint64_t> cptr_{0};
     std::vector<uint32_t> citems_;
+    std::vector<uint32_t> citems_orig_;   // citems_ as original ids, extended at each checkpoint
     std::vector<uint32_t> csup_;
     std::vector<double> ctime_;
     std::vector<uint32_t> cnode_;
@@ -600,8 +617,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         const double el = elapsed();
         while (next_ck < n_ckpt && el >= ckpts[next_ck]) {
             if (cb) {
-                std::vector<uint32_t> oi(citems_.size());
-                for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
+                for (size_t k = citems_orig_.size(); k < citems_.size(); ++k) citems_orig_.push_back(ds_.d2o[citems_[k]]);
+                const std::vector<uint32_t> &oi = citems_orig_;
                 sgfim_checkpoint ck;
                 ck.t_s = ckpts[next_ck];
                 ck.elapsed_s = el;
@@ -637,8 +654,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     // remaining checkpoints fire once the search is complete
     if (cb && next_ck < n_ckpt) {
         const double el = elapsed();
-        std::vector<uint32_t> oi(citems_.size());
-        for (size_t k = 0; k < citems_.size(); ++k) oi[k] = ds_.d2o[citems_[k]];
+        for (size_t k = citems_orig_.size(); k < citems_.size(); ++k) citems_orig_.push_back(ds_.d2o[citems_[k]]);
+        const std::vector<uint32_t> &oi = citems_orig_;
         for (; next_ck < n_ckpt; ++next_ck) {
             sgfim_checkpoint ck;
             ck.t_s = ckpts[next_ck];
@@ -666,19 +683,25 @@ int Miner::finish(sgfim_result **out) {
         const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
         const uint64_t chunk = 1u << 20;
         QuerySet qs;
-        std::vector<uint32_t> cnt, tmp;
+        std::vector<uint32_t> cnt;
         std::vector<uint64_t> w0;
         for (uint64_t a = 0; a < n; a += chunk) {
             const uint64_t b = std::min(n, a + chunk);
-            qs.clear();
-            w0.clear();
-            for (uint64_t c = a; c < b; ++c) {
-                tmp.assign(citems_.begin() + cptr_[c], citems_.begin() + cptr_[c + 1]);
-                std::sort(tmp.begin(), tmp.end(),
-                          [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
-                qs.add(tmp.data(), tmp.size(), kNoSlot);
-                w0.push_back(ccheck_[c] / 64);
-            }
+            // each candidate's items, rarest pool row first, built in parallel ranges
+            qs.ptr.resize(b - a + 1);
+            for (uint64_t c = a; c <= b; ++c) qs.ptr[c - a] = cptr_[c] - cptr_[a];
+            qs.items.resize(cptr_[b] - cptr_[a]);
+            qs.slot.assign(b - a, kNoSlot);
+            w0.resize(b - a);
+            parallel_ranges(b - a, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t c = a + lo; c < a + hi; ++c) {
+                    uint32_t *dst = qs.items.data() + (cptr_[c] - cptr_[a]);
+                    std::copy(citems_.begin() + cptr_[c], citems_.begin() + cptr_[c + 1], dst);
+                    std::sort(dst, dst + (cptr_[c + 1] - cptr_[c]),
+                              [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
+                    w0[c - a] = ccheck_[c] / 64;
+                }
+            });
             timed(3, [&] { run_queries(qs, pool_.as<uint64_t>(), pool_words_, pw, ds_.d, QUERY_ANY2, cnt, w0.data()); });
             for (uint64_t c = a; c < b; ++c) keep[c] = cnt[c - a] <= 1;
         }
@@ -713,12 +736,49 @@ int Miner::finish(sgfim_result **out) {
         }
         order.push_back(c);
     }
-    // deterministic order: support descending, then items lexicographic
-    std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
-        if (csup_[a] != csup_[b]) return csup_[a] > csup_[b];
-        return std::lexicographical_compare(citems_.begin() + cptr_[a], citems_.begin() + cptr_[a + 1],
-                                            citems_.begin() + cptr_[b], citems_.begin() + cptr_[b + 1]);
-    });
+    // deterministic order: support descending, then items lexicographic.  A stable LSD
+    // radix sort on the complemented support (four byte passes) makes runs of equal
+    // support; the runs are then sorted by items, in parallel ranges of runs.
+    if (n >= (1ull << 32)) {
+        std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+            if (csup_[a] != csup_[b]) return csup_[a] > csup_[b];
+            return std::lexicographical_compare(citems_.begin() + cptr_[a], citems_.begin() + cptr_[a + 1],
+                                                citems_.begin() + cptr_[b], citems_.begin() + cptr_[b + 1]);
+        });
+    } else {
+        // keys: complemented support above the candidate index (both 32 bits)
+        const uint64_t m0 = order.size();
+        std::vector<uint64_t> key(m0), tmp_k(m0);
+        for (uint64_t i = 0; i < m0; ++i) key[i] = ((uint64_t)(~csup_[order[i]]) << 32) | order[i];
+        uint64_t *src = key.data(), *dst = tmp_k.data();
+        for (int pass = 0; pass < 4; ++pass) {
+            const int sh = 32 + 8 * pass;
+            uint64_t cnt[257] = {0};
+            for (uint64_t i = 0; i < m0; ++i) ++cnt[(src[i] >> sh & 255u) + 1];
+            for (int k = 0; k < 256; ++k) cnt[k + 1] += cnt[k];
+            for (uint64_t i = 0; i < m0; ++i) dst[cnt[src[i] >> sh & 255u]++] = src[i];
+            std::swap(src, dst);
+        }
+        // four passes: the sorted keys are back in key[]
+        std::vector<uint64_t> runs{0};
+        for (uint64_t i = 0; i < m0; ++i) {
+            order[i] = key[i] & 0xffffffffull;
+            if (i && (key[i] >> 32) != (key[i - 1] >> 32)) runs.push_back(i);
+        }
+        runs.push_back(m0);
+        const uint64_t n_runs = runs.size() - 1;
+        auto lex = [&](uint64_t a, uint64_t b) {
+            return std::lexicographical_compare(citems_.begin() + cptr_[a], citems_.begin() + cptr_[a + 1],
+                                                citems_.begin() + cptr_[b], citems_.begin() + cptr_[b + 1]);
+        };
+        // ranges of elements, each sorting the runs that start inside it (runs of low
+        // supports are the long ones: splitting by run count would load one range)
+        parallel_ranges(m0, [&](uint64_t lo, uint64_t hi) {
+            uint64_t r = std::lower_bound(runs.begin(), runs.begin() + n_runs, lo) - runs.begin();
+            for (; r < n_runs && runs[r] < hi; ++r)
+                if (runs[r + 1] - runs[r] > 1) std::sort(order.begin() + runs[r], order.begin() + runs[r + 1], lex);
+        });
+    }
     sgfim_result *r = static_cast<sgfim_result *>(calloc(1, sizeof(sgfim_result)));
     if (!r) return fail(h_, SGFIM_ENOMEM, "result allocation failed");
     const uint64_t m = order.size();
@@ -739,14 +799,16 @@ int Miner::finish(sgfim_result **out) {
         return fail(h_, SGFIM_ENOMEM, "result allocation failed");
     }
     r->set_ptr[0] = 0;
-    uint64_t at = 0;
-    for (uint64_t i = 0; i < m; ++i) {
-        const uint64_t c = order[i];
-        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[at++] = ds_.d2o[citems_[k]];
-        r->set_ptr[i + 1] = at;
-        r->support[i] = csup_[c];
-        r->emit_time_s[i] = ctime_[c];
-    }
+    for (uint64_t i = 0; i < m; ++i) r->set_ptr[i + 1] = r->set_ptr[i] + (cptr_[order[i] + 1] - cptr_[order[i]]);
+    parallel_ranges(m, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            const uint64_t c = order[i];
+            uint64_t at = r->set_ptr[i];
+            for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[at++] = ds_.d2o[citems_[k]];
+            r->support[i] = csup_[c];
+            r->emit_time_s[i] = ctime_[c];
+        }
+    });
     if (tn) {
         memcpy(r->trace_features, tfeat_.data(), tn * kDim * 4);
         for (uint64_t t = 0; t < tn; ++t) r->trace_labels[t] = pos[tnode_[t]];

@@ -198,21 +198,26 @@ class WindowView:
 
 
 class WindowService:
-    """mode "batched": one scheduler thread hands every queued request to one
+    """mode "batched": `schedulers` threads (one by default), each with its own
+    handle; a free scheduler hands every queued request to one
     sgfim_ring_mine_windows call (a warp per root subtree of every window; the
-    handle's HBM budget bounds the per-warp workspaces and the output arena).  mode
+    handle's HBM budget bounds the per-warp workspaces and the output arena), so
+    with two a new batch starts while the previous one is still on the GPU.  mode
     "workers": `workers` threads, each with its own handle, mine one window at
     a time with the wave miner, admitted by a per-window memory estimate."""
 
     def __init__(self, workers=8, hbm_budget=8 << 30, device=0, ring_txn=WORKLOAD["ring_txn"], n_items=126,
-                 keep_results=False, mode="batched", max_batch=8192):
+                 keep_results=False, mode="batched", max_batch=8192, schedulers=1):
         if mode not in ("batched", "workers"):
             raise ValueError("mode must be 'batched' or 'workers'")
+        if schedulers < 1:
+            raise ValueError("schedulers must be >= 1")
         self.mode = mode
         self.max_batch = max_batch
         self.ring = Ring(n_items, ring_txn, device)
         if mode == "batched":
-            self.engines = [Engine(device=device, hbm_budget=hbm_budget, blocking_sync=True)]
+            self.engines = [Engine(device=device, hbm_budget=hbm_budget, blocking_sync=True)
+                            for _ in range(schedulers)]
         else:
             self.engines = [Engine(device=device, blocking_sync=True) for _ in range(workers)]
         self.budget = hbm_budget
@@ -466,6 +471,9 @@ def main(argv=None):
     ap.add_argument("--requests", type=int, default=WORKLOAD["n_req"])
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--mode", choices=("batched", "workers"), default="batched")
+    ap.add_argument("--schedulers", type=int, default=2,
+                    help="batched mode: concurrent batches (a handle and a thread each); measured at "
+                         "2,000 req/s: 1 -> p50 36.9 / p99 56.2 ms, 2 -> 32.9 / 52.5 ms, 3 -> 35.5 / 59.3 ms")
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     ap.add_argument("--check", action="store_true", help="compare every window with the oracle")
     ap.add_argument("--check-budget-s", type=float, default=240.0)
@@ -483,7 +491,7 @@ def main(argv=None):
     if a.saturate:
         return saturate(rows, reqs, a.saturate, a.horizontal, int(a.hbm_budget_gb * (1 << 30)), a.out)
     svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
-                        keep_results=a.check, mode=a.mode)
+                        keep_results=a.check, mode=a.mode, schedulers=a.schedulers)
     # warm-up pass on a handful of requests (first-use allocations of every worker)
     warm = make_requests(2 * a.workers, 4000.0, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=99)
     svc.run(rows, warm, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
@@ -497,7 +505,7 @@ def main(argv=None):
         if rq.error:
             errs[rq.error] = errs.get(rq.error, 0) + 1
     report = {"workload": "windows-4096", "requests": a.requests, "rate_hz": a.rate,
-              "workers": a.workers if a.mode == "workers" else 1,
+              "workers": a.workers if a.mode == "workers" else a.schedulers,
               "hbm_budget_gb": a.hbm_budget_gb, **rep, "error_kinds": errs,
               "config": {k: WORKLOAD[k] for k in WORKLOAD}}
     ctx = mp.get_context("spawn")

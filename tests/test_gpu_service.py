@@ -55,12 +55,16 @@ def test_ring_windows_match_slices(engine):
         ring.close()
 
 
-@pytest.mark.parametrize("mode", ["batched", "workers"])
-def test_service_windows_exact(mode):
+@pytest.mark.parametrize("mode,schedulers", [("batched", 1), ("batched", 3), ("workers", 1)])
+def test_service_windows_exact(mode, schedulers):
+    """Every window of a replayed request stream equals the oracle's MFIs: one
+    batch scheduler, three concurrent batch schedulers sharing the ring, and the
+    per-window workers."""
     from sgfim.service import WindowService, make_requests
     rows = datagen.regime_txns(200_000, 21, 6, 8, 0.3, seed=7)
     reqs = make_requests(48, 400.0, 512, 8192, seed=3)
-    svc = WindowService(workers=4, hbm_budget=2 << 30, ring_txn=1 << 16, keep_results=True, mode=mode)
+    svc = WindowService(workers=4, hbm_budget=2 << 30, ring_txn=1 << 16, keep_results=True, mode=mode,
+                        schedulers=schedulers)
     try:
         rep = svc.run(rows, reqs, stream_rate=20_000.0, floor_frac=0.05, warm_txn=8192)
     finally:

@@ -203,7 +203,7 @@ size_t wmine_root_bytes(int mw);
 void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wsub(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
-void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st);
+void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, unsigned threads, cudaStream_t st);
 void launch_wgather(const WGatherParams &p, int mw, unsigned blocks, cudaStream_t st);
 
 }  // namespace sg

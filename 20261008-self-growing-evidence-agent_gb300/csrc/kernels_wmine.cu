@@ -1165,7 +1165,7 @@ template <int MW> __global__ void __launch_bounds__(128, SGFIM_WVTASK_MIN_BLOCKS
 // in depth-first order) get a vertical bitmap rows[e][q]; candidate q of a
 // task is dropped when the AND of its items' rows has a bit below the task's
 // first candidate.  keep[] is written per arena slot, kept[] per task.
-template <int MW> __global__ void __launch_bounds__(256) wfilter_kernel(WFilterParams p) {
+template <int MW> __global__ void __launch_bounds__(1024) wfilter_kernel(WFilterParams p) {
     __shared__ uint32_t s_w;
     __shared__ uint32_t s_freq[64 * MW];              // candidates holding each item
     __shared__ uint32_t s_lo[64 * MW], s_hi[64 * MW];  // first / last word of each item's row with a bit
@@ -1318,9 +1318,11 @@ void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st
         wtask_kernel<2><<<blocks, 128, 0, st>>>(p);
     SG_CUDA_TRY(cudaGetLastError());
 }
-void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, cudaStream_t st) {
+void launch_wfilter(const WFilterParams &p, int mw, unsigned blocks, unsigned threads, cudaStream_t st) {
     if (mw != 2) throw CudaError(cudaErrorInvalidValue, "batched window miner supports 2 mask words", __FILE__, __LINE__);
-    wfilter_kernel<2><<<blocks, 256, 0, st>>>(p);
+    if (threads != 256 && threads != 1024)
+        throw CudaError(cudaErrorInvalidValue, "filter blocks are 256 or 1,024 threads", __FILE__, __LINE__);
+    wfilter_kernel<2><<<blocks, threads, 0, st>>>(p);
     SG_CUDA_TRY(cudaGetLastError());
 }
 void launch_wgather(const WGatherParams &p, int mw, unsigned blocks, cudaStream_t st) {

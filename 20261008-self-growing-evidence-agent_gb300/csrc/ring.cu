@@ -727,7 +727,9 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                     fp.win_status = d_wstat;
                     fp.next = ws.ctrl.as<uint32_t>() + 8;
                     SG_CUDA_TRY(cudaEventRecord(k0, st));
-                    launch_wfilter(fp, (int)mw, (unsigned)ctas, st);
+                    // few windows (a service batch): 1,024 threads per window's CTA, so the
+                    // largest window's candidates are scanned four times as wide
+                    launch_wfilter(fp, (int)mw, (unsigned)ctas, fwin.size() <= (size_t)h->n_sm * 2 ? 1024u : 256u, st);
                     SG_CUDA_TRY(cudaEventRecord(k1, st));
                     ++launches;
                     ++h->launches;

@@ -10,6 +10,7 @@
 // extracted by a funnel-shift copy into a handle's dataset, so no window is
 // ever transposed on the host.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <mutex>
@@ -532,6 +533,19 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             // ---- 3. tasks in depth-first order within each window
             std::vector<uint32_t> t_win, t_child, t_sub, t_gchild;
             std::vector<double> t_cost;
+            {
+                size_t est = n_windows;
+                for (uint32_t w : split) {
+                    const unsigned char *R = root_at(w);
+                    if (!u32_at(R, o_has)) est += u32_at(R, o_k);
+                }
+                for (size_t i = 0; i < sub_win.size(); ++i) est += u32_at(subs_h.data() + i * root_b, o_k);
+                t_win.reserve(est);
+                t_child.reserve(est);
+                t_sub.reserve(est);
+                t_gchild.reserve(est);
+                t_cost.reserve(est);
+            }
             auto add_task = [&](uint32_t w, uint32_t c, uint32_t sb, uint32_t g, double cost) {
                 t_win.push_back(w);
                 t_child.push_back(c);
@@ -579,7 +593,20 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
             n_tasks_total = nt;
             std::vector<uint32_t> order(nt);
             for (uint64_t i = 0; i < nt; ++i) order[i] = (uint32_t)i;
-            std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return t_cost[x] > t_cost[y]; });
+            // costliest first to within a factor of two (a counting sort on the cost's binary
+            // exponent, creation order inside an exponent): the order only schedules the tasks
+            {
+                std::vector<uint32_t> bucket(nt);
+                uint64_t cnt[129] = {0};
+                for (uint64_t i = 0; i < nt; ++i) {
+                    int e = 0;
+                    std::frexp(t_cost[i], &e);
+                    bucket[i] = 127u - (uint32_t)std::min(127, std::max(0, e));
+                    ++cnt[bucket[i] + 1];
+                }
+                for (int b = 0; b < 128; ++b) cnt[b + 1] += cnt[b];
+                for (uint64_t i = 0; i < nt; ++i) order[cnt[bucket[i]]++] = (uint32_t)i;
+            }
             // task arrays: win | child | sub | gchild | order | cnt | kept | status (u32) | off | nodes (u64)
             const size_t nt1 = std::max<uint64_t>(nt, 1);
             const size_t u32_bytes = (8 * 4 * nt1 + 15) & ~(size_t)15;

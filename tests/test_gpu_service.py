@@ -182,3 +182,27 @@ def test_mine_windows_wide_ring_uses_wave_miner(engine):
         assert masks_to_sets(np.array([[1, 0, 0, 1 << 3]], np.uint64)) == [(0, 195)]
     finally:
         ring.close()
+
+
+def test_ring_mine_windows_many_windows_filter_layout():
+    """More split windows than two per SM: the cross-subtree filter runs 256-thread
+    CTAs (1,024-thread ones below that count); every window still equals the oracle."""
+    from sgfim.engine import Engine
+    from sgfim.service import Ring
+    rows = datagen.regime_txns(40_000, 21, 6, 8, 0.3, seed=23)
+    rp, it = datagen.txns_to_csr(rows)
+    ring = Ring(126, 1 << 16)
+    engine = Engine()
+    try:
+        ring.append(rp, it)
+        rng = np.random.default_rng(8)
+        lens = [int(x) for x in rng.integers(64, 1500, 420)]
+        starts = [int(rng.integers(0, len(rows) - L)) for L in lens]
+        thrs = [max(1, int(np.ceil(0.04 * L))) for L in lens]
+        res = ring.mine_windows(engine, starts, lens, thrs)
+        assert (res.status == 0).all() and res.batched.all()
+        for w, (s, L, thr) in enumerate(zip(starts, lens, thrs)):
+            assert res.as_dict(w) == _oracle_mfis(rows[s:s + L], thr), (w, s, L, thr)
+    finally:
+        ring.close()
+        engine.close()

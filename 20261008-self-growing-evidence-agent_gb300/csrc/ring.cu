@@ -43,6 +43,8 @@ struct sgfim_ring {
 #define SGFIM_WFILTER_CTAS_PER_SM 8
 #endif
 constexpr uint64_t kFilterCtasPerSm = SGFIM_WFILTER_CTAS_PER_SM;
+// results up to this size leave the device through a pinned staging buffer
+constexpr size_t kStageOutMax = 64ull << 20;
 
 namespace sg {
 
@@ -899,9 +901,24 @@ int sgfim_ring_mine_windows(sgfim_ring *r, sgfim_handle *h, const uint64_t *star
                                st);
                 ++launches;
                 ++h->launches;
-                SG_CUDA_TRY(cudaMemcpyAsync(R->masks, d_dst_m, at * mw * 8, cudaMemcpyDeviceToHost, st));
-                SG_CUDA_TRY(cudaMemcpyAsync(R->support, d_dst_s, at * 4, cudaMemcpyDeviceToHost, st));
-                h->sync();
+                const size_t out_b = at * mw * 8 + at * 4;
+                if (out_b <= kStageOutMax && words == mw) {
+                    // small results through the handle's pinned staging buffer: the copy into the
+                    // freshly allocated (pageable) result arrays would fault their pages in
+                    // during the DMA
+                    ws2.h_out.reserve(out_b);
+                    uint64_t *h_m = ws2.h_out.as<uint64_t>();
+                    uint32_t *h_s = reinterpret_cast<uint32_t *>(h_m + at * mw);
+                    SG_CUDA_TRY(cudaMemcpyAsync(h_m, d_dst_m, at * mw * 8, cudaMemcpyDeviceToHost, st));
+                    SG_CUDA_TRY(cudaMemcpyAsync(h_s, d_dst_s, at * 4, cudaMemcpyDeviceToHost, st));
+                    h->sync();
+                    memcpy(R->masks, h_m, at * mw * 8);
+                    memcpy(R->support, h_s, at * 4);
+                } else {
+                    SG_CUDA_TRY(cudaMemcpyAsync(R->masks, d_dst_m, at * mw * 8, cudaMemcpyDeviceToHost, st));
+                    SG_CUDA_TRY(cudaMemcpyAsync(R->support, d_dst_s, at * 4, cudaMemcpyDeviceToHost, st));
+                    h->sync();
+                }
             }
         }
     } catch (const CudaError &e) {

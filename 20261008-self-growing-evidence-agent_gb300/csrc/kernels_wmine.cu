@@ -596,7 +596,9 @@ template <int MW> __global__ void __launch_bounds__(128) wsub_kernel(WMineParams
         WRoot<MW> &S = subs[si];
         uint32_t n1 = 0, overflow = 0;
         if (m_nz(T)) {
-            n1 = build_child<MW>(true, p, start, lists, 0, n, req, T, 0, lane);
+            // the child's database through the ring's row of item e: only the window's
+            // transactions holding e have their item masks read
+            n1 = build_base<MW>(p, start, n, req, T, lists, lane);
             if (n1 == 0xffffffffu) {
                 overflow = 1;
                 n1 = 0;

@@ -199,7 +199,7 @@ struct WGatherParams {
 };
 size_t wmine_level_bytes(int mw);
 size_t wmine_root_bytes(int mw);
-// blocks of 128 threads (4 warps; wfilter: 256 threads)
+// blocks of 128 threads (4 warps; wfilter: 256 or 1,024 threads)
 void launch_wroot(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wsub(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);
 void launch_wtask(const WMineParams &p, int mw, unsigned blocks, cudaStream_t st);

@@ -6,11 +6,15 @@
 // window's transactions at the window's floor, which these kernels reproduce.
 //
 // Representation.  Items are the ring's dense ids 0..d-1 (d <= 64*MW); an
-// itemset is an MW-word mask.  A search node (H, T) holds its projected
-// database: one MW-word entry per transaction of t(H) that still contains a
-// tail item, restricted to T (transactions whose restriction is empty add
-// nothing to any count below the node and are dropped).  The root's database
-// is the window itself, read from the ring's horizontal masks.
+// itemset is an MW-word mask.  A task's base database holds one MW-word entry
+// per window transaction that contains the task's required items and still
+// holds a tail item, restricted to the tail (build_base: the transactions are
+// found through the ring's vertical rows, their item masks read from the
+// ring's horizontal masks).  wvtask_kernel (the default) turns the base into
+// vertical rows, one bit per entry per item, and keeps one tidset per search
+// level: counts are AND-popcounts of the level's tidset with the item rows.
+// wtask_kernel (SGFIM_F_WINDOWS_HORIZONTAL) instead stacks each level's
+// projected database as entries.
 //
 // Search.  Depth-first over the set-enumeration tree, one node at a time per
 // warp, children in ascending (support, id) order -- the order under which a
@@ -27,14 +31,16 @@
 // containing the child's head, plus everything found inside the parent's
 // subtree, which contains the parent's head by construction).
 //
-// Work split.  A short window is one task: its warp searches the whole tree
-// and its pool is the exact MFI set.  A long window is split at the root:
-// wroot_kernel counts the root and sorts its frequent tail f_0..f_{k-1};
-// task (w, j) searches child j's subtree alone.  Tasks share no pool, so a
-// candidate of subtree j may sit inside a candidate of an earlier subtree
-// i < j (never of a later one, by the argument above); wfilter_kernel removes
-// exactly those with a vertical bitmap of the window's candidates.
-// wgather_kernel then writes the kept candidates in window order.
+// Work split.  A window shorter than 64 transactions is one task: its warp
+// searches the whole tree and its pool is the exact MFI set.  Longer windows
+// are split at the root: wroot_kernel counts the root and sorts its frequent
+// tail f_0..f_{k-1}; task (w, j) searches child j's subtree alone.  The
+// costliest children are split once more (wsub_kernel expands child j the same
+// way; task (w, j, g) searches its child g).  Tasks share no pool, so a
+// candidate of one subtree may sit inside a candidate of an earlier subtree
+// in depth-first order (never of a later one, by the argument above);
+// wfilter_kernel removes exactly those with a vertical bitmap of the window's
+// candidates, and wgather_kernel writes the kept candidates in window order.
 //
 // Work is distributed by atomic counters (costliest tasks first); every
 // loop is bounded by list lengths, and any capacity overflow (entry stack,

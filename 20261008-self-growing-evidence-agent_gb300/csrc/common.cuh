@@ -23,7 +23,16 @@ enum : uint32_t {
 namespace sg {
 
 constexpr int kWarp = 32;
-constexpr uint32_t kMbarSpinLimit = 1u << 26;  // ~ seconds of polling; never unbounded
+
+// Device control words.  Every kernel that can wait receives `err`, a pointer
+// to a small device block: err[kCtlCode] holds the first error code, and
+// err[kCtlWaitUs] the bound of every mbarrier wait in microseconds of
+// %globaltimer (0 = kWaitLimitUsDefault).  A wait that runs out records
+// DEVERR_MBAR_TIMEOUT and the kernel leaves; the host reads and clears the
+// code after the launch.
+constexpr int kCtlCode = 0;
+constexpr int kCtlWaitUs = 1;
+constexpr uint32_t kWaitLimitUsDefault = 4000000;  // 4 s
 
 // ------------------------------------------------------------------ device helpers
 __device__ __forceinline__ uint32_t popc64(uint64_t x) { return (uint32_t)__popcll(x); }
@@ -66,11 +75,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: returns false (and records DEVERR_MBAR_TIMEOUT) after
-// kMbarSpinLimit polls instead of spinning forever.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: polls until the phase completes or err[kCtlWaitUs]
+// microseconds (kWaitLimitUsDefault when 0 or err is null) have passed on the
+// global timer, then records DEVERR_MBAR_TIMEOUT and returns false.  The
+// clock is only read once the first poll has failed.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err) {
-    for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    uint32_t us = err ? *reinterpret_cast<volatile uint32_t *>(err + kCtlWaitUs) : 0u;
+    if (us == 0) us = kWaitLimitUsDefault;
+    const uint64_t t0 = global_ns(), limit = (uint64_t)us * 1000ull;
+    for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > limit) break;
     }
     set_device_error(err, DEVERR_MBAR_TIMEOUT);
     return false;

@@ -117,6 +117,9 @@ int sgfim_open(const sgfim_config *cfg, sgfim_handle **out) {
     h->flags = cfg ? cfg->flags : 0;
     h->dev_err.reserve(256, h->stream);
     SG_CUDA_TRY(cudaMemsetAsync(h->dev_err.ptr, 0, 256, h->stream));
+    const uint32_t wait_us = cfg ? cfg->wait_limit_us : 0u;
+    SG_CUDA_TRY(cudaMemcpyAsync(h->dev_err.as<uint32_t>() + kCtlWaitUs, &wait_us, 4, cudaMemcpyHostToDevice,
+                                h->stream));
     SG_CUDA_TRY(cudaStreamSynchronize(h->stream));
     *out = h;
     return SGFIM_OK;
@@ -156,6 +159,31 @@ void sgfim_close(sgfim_handle *h) {
 }
 
 const char *sgfim_last_error(const sgfim_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+int sgfim_device_status(sgfim_handle *h, void *stream) {
+    if (!h) return SGFIM_EINVAL;
+    API_GUARD_BEGIN
+    cudaSetDevice(h->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (cudaStream_t)0;
+    uint32_t e = 0;
+    SG_CUDA_TRY(cudaMemcpyAsync(&e, h->dev_err.as<uint32_t>() + kCtlCode, 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (e == DEVERR_NONE) return SGFIM_OK;
+    SG_CUDA_TRY(cudaMemsetAsync(h->dev_err.as<uint32_t>() + kCtlCode, 0, 4, st));
+    SG_CUDA_TRY(cudaStreamSynchronize(st));
+    return fail(h, SGFIM_EDEVICE, "device wait or bounds check failed (code " + std::to_string(e) + ")");
+    API_GUARD_END(h)
+}
+
+int sgfim_selftest_wait(sgfim_handle *h) {
+    if (!h) return SGFIM_EINVAL;
+    API_GUARD_BEGIN
+    cudaSetDevice(h->device);
+    launch_wait_probe(h->dev_err.as<uint32_t>(), h->stream);
+    ++h->launches;
+    return check_device_error(h);
+    API_GUARD_END(h)
+}
 
 }  // extern "C"
 
@@ -427,7 +455,7 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
 
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves) {
     if (!h) return SGFIM_EINVAL;
-    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_STAGED4) return fail(h, SGFIM_EINVAL, "unknown kernel");
+    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_LANE) return fail(h, SGFIM_EINVAL, "unknown kernel");
     h->plan.kernel = kernel;
     h->plan.cands_per_cta = cands_per_cta;
     h->plan.waves = waves;

@@ -58,7 +58,8 @@ void launch_tail_counts(const uint64_t *rows, uint64_t row_stride, uint64_t n_wo
 // into 16-byte records when every item fits 16 bits and k <= 8, runs the
 // shared-memory staged kernel on those and the streaming kernel on the rest.
 enum SupportKernel : int {
-    SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3, SUPPORT_STAGED4 = 4
+    SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3, SUPPORT_STAGED4 = 4,
+    SUPPORT_LANE = 5
 };
 struct SupportPlan {
     int kernel = SUPPORT_AUTO;
@@ -86,10 +87,25 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
                          uint32_t *out, const SupportScratch &scratch, const SupportPlan &plan,
                          const CUtensorMap *map, uint32_t *dev_err, cudaStream_t st, int n_sm,
                          uint64_t *launches, cudaEvent_t *ev = nullptr);
+// One lane per candidate (kernels_lane.cu): k-sorted records, chunks staged by
+// TMA.  Returns -1 when d or the shared-memory layout does not fit (the caller
+// then takes another kernel); otherwise the >8-item candidates are left in
+// *ovf_list / *ovf_count (device) for the streaming kernel.  ev (optional):
+// ev[1] and ev[2] are recorded around the counting kernel.
+bool lane_supported(uint32_t d);
+int lane_supports_device(const CUtensorMap *map, uint32_t d, uint64_t n_words, const uint64_t *cand_ptr,
+                         const uint32_t *cand_items, uint64_t n_cand, uint64_t n_txn, uint32_t *out, void *scratch,
+                         size_t scratch_bytes, uint32_t waves, uint32_t *dev_err, cudaStream_t st, int n_sm,
+                         uint32_t **ovf_list, unsigned long long **ovf_count, uint64_t *launches,
+                         cudaEvent_t *ev);
 // Encode the 2-D tensor map used by the staged kernel (rows x words, u64).
 bool encode_bitmap_map(CUtensorMap *map, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
                        uint64_t row_stride);
 size_t staged_smem_bytes(uint32_t d, uint32_t cands_per_cta);
+
+// A kernel whose mbarrier never completes: its bounded wait runs out and
+// records DEVERR_MBAR_TIMEOUT in err (the wait self-test).
+void launch_wait_probe(uint32_t *err, cudaStream_t st);
 
 // Miner helpers.
 // mask(child c) = (parent_slot[c] != kNoSlot ? arena[parent_slot[c]] : ones) & AND rows(items[ptr[c]..ptr[c+1]))

@@ -817,7 +817,27 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     if (map == nullptr || d == 0) kind = SUPPORT_STREAM;
     // measured on GB300 at 1M candidates x 1,024 rows: staged with 4-lane groups 30.0 ms,
     // staged with 8-lane groups 30.9 ms, sorted 30.8-46 ms (depending on its grid)
-    if (kind == SUPPORT_AUTO) kind = SUPPORT_STAGED4;
+    if (kind == SUPPORT_AUTO) kind = lane_supported(d) ? SUPPORT_LANE : SUPPORT_STAGED4;
+    if (kind == SUPPORT_LANE) {
+        uint32_t *ovf_l = nullptr;
+        unsigned long long *ovf_c = nullptr;
+        mark(0);
+        const int rc = lane_supports_device(map, d, n_words_even, cand_ptr, cand_items, n_cand, n_txn, out,
+                                            scratch.base, scratch.bytes, plan.waves ? plan.waves : 2, dev_err, st,
+                                            n_sm, &ovf_l, &ovf_c, launches, ev);
+        if (rc == 0) {
+            QueryBatch qb;
+            qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;
+            qb.q_ptr = cand_ptr; qb.q_items = cand_items; qb.n_q_device = reinterpret_cast<const uint64_t *>(ovf_c);
+            qb.q_index = ovf_l; qb.out = out; qb.empty_value = n_txn;
+            launch_queries(qb, st, n_sm);
+            mark(3);
+            if (launches) *launches += 1;
+            return 0;
+        }
+        if (scratch.bytes < support_scratch_bytes(n_cand)) return -1;
+        kind = SUPPORT_STAGED4;
+    }
     if (kind == SUPPORT_SORTED && d > kSortCompactMax) kind = SUPPORT_STAGED;
     if ((kind == SUPPORT_STAGED || kind == SUPPORT_STAGED4) && d > 65535) kind = SUPPORT_STREAM;
     uint32_t cpc = 0;
@@ -897,6 +917,25 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     mark(3);
     if (launches) *launches += 1;
     return 0;
+}
+
+// ---------------------------------------------------------------- wait self-test
+// An mbarrier that nothing ever arrives at: every thread's bounded wait runs
+// out, records DEVERR_MBAR_TIMEOUT and returns.  No copy or MMA is issued, so
+// nothing is in flight when the CTA leaves.
+__global__ void wait_probe_kernel(uint32_t *err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    mbar_wait_bounded(&bar, 0, err);
+}
+
+void launch_wait_probe(uint32_t *err, cudaStream_t st) {
+    wait_probe_kernel<<<1, 32, 0, st>>>(err);
+    SG_CUDA_TRY(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------- miner helpers

@@ -14,6 +14,9 @@
 // array (kNoAllocScratchBytes, about 25 MB) until the process exits; inputs
 // larger than SGFIM_NOALLOC_MAX_CAND candidates are rejected; and all calls
 // share the one array, so calls that overlap on the GPU race.
+//
+// Device errors (a bounded wait that ran out) land in a second file-scope
+// word that stays set until sgfim_noalloc_status reads and clears it.
 #include <mutex>
 
 #include "common.cuh"
@@ -27,6 +30,7 @@ constexpr uint64_t kMaxCand = SGFIM_NOALLOC_MAX_CAND;
 constexpr size_t kNoAllocScratchBytes = sg::support_scratch_bytes_for(kMaxCand);
 
 __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
+// [sg::kCtlCode] error code, [sg::kCtlWaitUs] wait bound (0 = default); zero at load
 __device__ __align__(256) uint32_t g_dev_err[64];
 
 struct DeviceSlot {
@@ -83,6 +87,8 @@ extern "C" int sgfim_support_batch_noalloc(const uint64_t *bitmaps, uint32_t d, 
         sg::SupportScratch sc{slot->scratch, kNoAllocScratchBytes};
         sg::SupportPlan plan;
         cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (cudaStream_t)0;
+        // The only non-zero return is a scratch area smaller than the layout of
+        // n_cand candidates, which the size check above already rules out.
         if (sg::support_batch_device(bitmaps, d, n_even, row_stride, n_words * 64, cand_ptr, cand_items, n_cand, out,
                                      sc, plan, map_ok ? &map : nullptr, slot->err, st, slot->n_sm, nullptr) != 0)
             return SGFIM_ECAPACITY;
@@ -90,4 +96,22 @@ extern "C" int sgfim_support_batch_noalloc(const uint64_t *bitmaps, uint32_t d, 
     } catch (const sg::CudaError &) {
         return SGFIM_EDEVICE;
     }
+}
+
+extern "C" int sgfim_noalloc_status(void *stream) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SGFIM_EDEVICE;
+    DeviceSlot *slot = nullptr;
+    int rc = setup_device(dev, &slot);
+    if (rc != SGFIM_OK) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (cudaStream_t)0;
+    uint32_t code = 0;
+    // a copy into pageable host memory returns once it has completed
+    if (cudaMemcpyAsync(&code, slot->err + sg::kCtlCode, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return SGFIM_EDEVICE;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SGFIM_EDEVICE;
+    if (code == DEVERR_NONE) return SGFIM_OK;
+    if (cudaMemsetAsync(slot->err + sg::kCtlCode, 0, 4, st) != cudaSuccess) return SGFIM_EDEVICE;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SGFIM_EDEVICE;
+    return SGFIM_EDEVICE;
 }

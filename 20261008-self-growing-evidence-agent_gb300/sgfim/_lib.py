@@ -29,7 +29,7 @@ COOC_AUTO, COOC_POPC, COOC_BMMA, COOC_TC_F8 = 0, 1, 2, 3
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_uint64), ("wave_nodes", C.c_uint32),
-                ("flags", C.c_uint32), ("tune_cache", C.c_char_p)]
+                ("flags", C.c_uint32), ("tune_cache", C.c_char_p), ("wait_limit_us", C.c_uint32)]
 
 
 class DatasetInfo(C.Structure):
@@ -99,6 +99,9 @@ SIGNATURES = {
     "sgfim_open": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
     "sgfim_close": (None, [C.c_void_p]),
     "sgfim_last_error": (C.c_char_p, [C.c_void_p]),
+    "sgfim_device_status": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sgfim_selftest_wait": (C.c_int, [C.c_void_p]),
+    "sgfim_noalloc_status": (C.c_int, [C.c_void_p]),
     "sgfim_load_fimi": (C.c_int, [C.c_void_p, C.c_char_p]),
     "sgfim_load_csr": (C.c_int, [C.c_void_p, u64p, u32p, C.c_uint64]),
     "sgfim_load_bitmaps": (C.c_int, [C.c_void_p, u64p, C.c_uint32, C.c_uint64, C.c_uint64]),

@@ -81,12 +81,12 @@ class MineResult:
 
 class Engine:
     def __init__(self, device=0, hbm_budget=0, wave_nodes=0, verbose=False, phase_timers=False,
-                 ignore_id0=False, blocking_sync=False, windows_horizontal=False):
+                 ignore_id0=False, blocking_sync=False, windows_horizontal=False, wait_limit_us=0):
         self._L = L.load()
         flags = (L.F_VERBOSE if verbose else 0) | (L.F_PHASE_TIMERS if phase_timers else 0) | \
             (L.F_IGNORE_ID0 if ignore_id0 else 0) | (L.F_BLOCKING_SYNC if blocking_sync else 0) | \
             (L.F_WINDOWS_HORIZONTAL if windows_horizontal else 0)
-        cfg = L.Config(device, hbm_budget, wave_nodes, flags, None)
+        cfg = L.Config(device, hbm_budget, wave_nodes, flags, None, wait_limit_us)
         h = C.c_void_p()
         rc = self._L.sgfim_open(C.byref(cfg), C.byref(h))
         if rc != 0:
@@ -120,6 +120,16 @@ class Engine:
     @property
     def handle(self):
         return self._h
+
+    def device_status(self, stream=0):
+        """sgfim_device_status: 0, or SGFIM_EDEVICE when a device-pointer call since the
+        last check gave up on a bounded wait (the error word is cleared)."""
+        return int(self._L.sgfim_device_status(self._h, C.c_void_p(stream)))
+
+    def selftest_wait(self):
+        """sgfim_selftest_wait: a kernel whose wait can never complete; returns the
+        call's code (SGFIM_EDEVICE when the bound works)."""
+        return int(self._L.sgfim_selftest_wait(self._h))
 
     # ------------------------------------------------------------ loading
     def load_fimi(self, path):
@@ -244,7 +254,7 @@ class Engine:
         self._check(self._L.sgfim_support_batch_device(self._h, bm_ptr, d, n_words, row_stride, cand_ptr_ptr,
                                                        cand_items_ptr, n_cand, out_ptr, stream or None))
 
-    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3, "staged4": 4}
+    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3, "staged4": 4, "lane": 5}
 
     def set_support_plan(self, kernel="auto", cands_per_cta=0, waves=0):
         """Choose the support-batch kernel and its CTA sizing (see sgfim_support_plan_set)."""

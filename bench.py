@@ -54,7 +54,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cooc", action="store_true")
-    ap.add_argument("--kernel", choices=["auto", "sorted", "staged", "staged4", "stream"], default="auto")
+    ap.add_argument("--kernel", choices=["auto", "lane", "sorted", "staged", "staged4", "stream"], default="auto")
     ap.add_argument("--workload", choices=["support-1m", "transact-1m"], default="support-1m",
                     help="transact-1m: the sensor-stream front end (quantile and online P2 "
                          "transactionisation of 1M-row streams) instead of the support bench")

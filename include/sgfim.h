@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define SGFIM_ABI_VERSION 1
+#define SGFIM_ABI_VERSION 2
 
 enum {
     SGFIM_OK = 0,
@@ -57,6 +57,10 @@ typedef struct {
     uint32_t wave_nodes;      /* search nodes expanded per wave; 0 = engine default */
     uint32_t flags;           /* SGFIM_F_* */
     const char *tune_cache;   /* autotuner cache file (JSON); NULL = none */
+    uint32_t wait_limit_us;   /* bound of every device-side wait (an mbarrier that a TMA copy or an
+                                 MMA completes), in microseconds of the GPU's global timer; a wait
+                                 that runs out ends its kernel and the call returns SGFIM_EDEVICE.
+                                 0 = 4,000,000 (4 s) */
 } sgfim_config;
 
 #define SGFIM_F_VERBOSE 0x1u   /* print phase timers to stderr */
@@ -76,6 +80,22 @@ int sgfim_open(const sgfim_config *cfg, sgfim_handle **out);
 void sgfim_close(sgfim_handle *h);
 const char *sgfim_last_error(const sgfim_handle *h);
 int sgfim_abi_version(void);
+
+/* Device status of the asynchronous device-pointer calls
+ * (sgfim_support_batch_device, sgfim_cooccurrence_device): waits for
+ * `stream`, then reads and clears the handle's device error word.  Returns
+ * SGFIM_OK, or SGFIM_EDEVICE when a kernel launched since the last check gave
+ * up (a bounded wait ran out): the outputs of those calls are then
+ * incomplete.  The calls with host buffers check it themselves.  The
+ * reference has no counterpart: its kernels never wait on the device. */
+int sgfim_device_status(sgfim_handle *h, void *stream);
+
+/* Self-test of the bounded waits (no reference counterpart): launches one
+ * small kernel whose mbarrier nothing ever completes, so its wait runs out
+ * after the handle's wait_limit_us and records a device error.  Returns
+ * SGFIM_EDEVICE (the expected result) and leaves the handle usable; use a
+ * short wait_limit_us (milliseconds) for it. */
+int sgfim_selftest_wait(sgfim_handle *h);
 
 /* ---------------------------------------------------------------- loading */
 
@@ -146,11 +166,13 @@ int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
  * kernel: SGFIM_KERNEL_*; cands_per_cta: candidates a CTA owns (0 = derived);
  * waves: CTAs per SM over the grid when cands_per_cta is 0 (0 = the kernel's
  * default: 1 for SORTED, 2 for STAGED). */
-#define SGFIM_KERNEL_AUTO 0    /* STAGED4 when it fits shared memory, else streaming */
+#define SGFIM_KERNEL_AUTO 0    /* LANE when the rows fit shared memory (d <= 1,792), else STAGED4 or streaming */
 #define SGFIM_KERNEL_STAGED 1  /* TMA-staged chunks, candidates in input order */
 #define SGFIM_KERNEL_SORTED 2  /* TMA-staged chunks, candidates sorted by (k, first item); ids < 1024 */
 #define SGFIM_KERNEL_STREAM 3  /* one warp per candidate, rows streamed from L2/HBM */
 #define SGFIM_KERNEL_STAGED4 4 /* TMA-staged chunks, 4-lane groups (32 bytes of a row per lane) */
+#define SGFIM_KERNEL_LANE 5    /* TMA-staged chunks, one lane per candidate, candidates sorted by k
+                                  on the device; waves = CTAs per SM (default 2) */
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves);
 
 /* Allocation-free form of sgfim_support_batch_device.  It has no counterpart
@@ -174,6 +196,16 @@ int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, 
 int sgfim_support_batch_noalloc(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride,
                                 const uint64_t *cand_ptr, const uint32_t *cand_items, uint64_t n_cand,
                                 uint32_t *out, void *stream);
+
+/* Device status of sgfim_support_batch_noalloc on the current device: waits
+ * for `stream`, reads the library's fixed device error word and clears it.
+ * SGFIM_OK, or SGFIM_EDEVICE when one of the calls since the last check gave
+ * up on a bounded wait (its supports are then incomplete).  The word is shared
+ * by every call on the device and stays set until this call reads it.  It
+ * allocates nothing.  A device reset (cudaDeviceReset) unloads the library's
+ * device arrays: after one, neither no-alloc call may be used again in the
+ * process. */
+int sgfim_noalloc_status(void *stream);
 
 /* Phase timers (CUDA events on the launching stream) of the batched support
  * path, enabled by SGFIM_F_PHASE_TIMERS; the counterpart of the wave engine's

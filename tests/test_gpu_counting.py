@@ -18,6 +18,8 @@ def _bitmaps(n_txn, d, seed, lo=0.02, hi=0.3):
     (4096, 40, 3000, 1, 8),             # single-chunk bitmaps, k=1..8
     (64 * 1000 + 64, 300, 5000, 2, 6),  # odd word count, d not a multiple of 256
     (128 * 64, 1024, 9000, 3, 8),       # four TMA boxes
+    (8192 + 64, 1792, 40000, 1, 8),     # the widest lane layout (seven boxes)
+    (8192, 1800, 3000, 2, 9),           # too wide for the lane layout: another kernel
 ])
 def test_support_batch_matches_oracle(engine, n_txn, d, n_cand, kmin, kmax):
     bm = _bitmaps(n_txn, d, seed=n_txn + d)
@@ -28,7 +30,7 @@ def test_support_batch_matches_oracle(engine, n_txn, d, n_cand, kmin, kmax):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("kernel", ["sorted", "staged", "staged4", "stream"])
+@pytest.mark.parametrize("kernel", ["lane", "sorted", "staged", "staged4", "stream"])
 @pytest.mark.parametrize("d", [1024, 300])
 def test_support_kernels_agree(engine, kernel, d):
     """Every kernel plan gives the oracle's supports (k = 0..12, unknown ids included)."""

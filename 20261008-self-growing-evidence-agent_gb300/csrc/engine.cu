@@ -137,6 +137,9 @@ void sgfim_close(sgfim_handle *h) {
     h->ds.bitmaps.release();
     h->ds.remap.release();
     h->ds.sup_dev.release();
+    h->ds.ext_cooc.release();
+    h->ds.ext_d2o.release();
+    h->ext.release();
     h->support_scratch.release();
     h->cand_ptr_dev.release();
     h->cand_items_dev.release();
@@ -455,7 +458,7 @@ int sgfim_support_batch(sgfim_handle *h, const uint64_t *cand_ptr, const uint32_
 
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves) {
     if (!h) return SGFIM_EINVAL;
-    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_LANE) return fail(h, SGFIM_EINVAL, "unknown kernel");
+    if (kernel < SGFIM_KERNEL_AUTO || kernel > SGFIM_KERNEL_LANE_TM) return fail(h, SGFIM_EINVAL, "unknown kernel");
     h->plan.kernel = kernel;
     h->plan.cands_per_cta = cands_per_cta;
     h->plan.waves = waves;

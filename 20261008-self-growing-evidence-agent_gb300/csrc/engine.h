@@ -56,16 +56,21 @@ struct Dataset {
     CUtensorMap map{};
     bool map_ok = false;
     std::string source;          // file name or "<memory>"
+    // sgfim_frequent_extensions: the rows' co-occurrence matrix and dense -> original ids
+    DevBuf ext_cooc, ext_d2o;
+    bool ext_cooc_ready = false;
 };
 
 // Forget a dataset's contents but keep its device buffers for the next load
 // (DevBuf has no destructor: assigning a fresh Dataset would leak them).
 inline void reset_dataset(Dataset &ds) {
-    const DevBuf bm = ds.bitmaps, remap = ds.remap, sup = ds.sup_dev;
+    const DevBuf bm = ds.bitmaps, remap = ds.remap, sup = ds.sup_dev, cooc = ds.ext_cooc, d2o = ds.ext_d2o;
     ds = Dataset{};
     ds.bitmaps = bm;
     ds.remap = remap;
     ds.sup_dev = sup;
+    ds.ext_cooc = cooc;
+    ds.ext_d2o = d2o;
 }
 
 // A device copy staged through a pinned host buffer (both grow, never shrink).
@@ -145,6 +150,19 @@ struct MinerWorkspace {
     }
 };
 
+// Buffers of sgfim_frequent_extensions, kept by the handle across calls.
+struct ExtWorkspace {
+    DevBuf list, n_list, out;
+    Staged ptr, rows;
+    void release() {
+        list.release();
+        n_list.release();
+        out.release();
+        ptr.release();
+        rows.release();
+    }
+};
+
 // MLP scorer weights (device) for the learned frontier order.
 struct Scorer {
     bool loaded = false;
@@ -169,6 +187,7 @@ struct sgfim_handle {
     sg::DevBuf cooc_scratch;
     sg::MinerWorkspace mws;
     sg::WindowWorkspace wws;
+    sg::ExtWorkspace ext;
     sg::SupportPlan plan;
     uint64_t launches = 0;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;

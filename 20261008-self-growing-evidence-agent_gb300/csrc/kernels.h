@@ -59,7 +59,7 @@ void launch_tail_counts(const uint64_t *rows, uint64_t row_stride, uint64_t n_wo
 // shared-memory staged kernel on those and the streaming kernel on the rest.
 enum SupportKernel : int {
     SUPPORT_AUTO = 0, SUPPORT_STAGED = 1, SUPPORT_SORTED = 2, SUPPORT_STREAM = 3, SUPPORT_STAGED4 = 4,
-    SUPPORT_LANE = 5
+    SUPPORT_LANE = 5, SUPPORT_LANE_TM = 6
 };
 struct SupportPlan {
     int kernel = SUPPORT_AUTO;
@@ -93,6 +93,13 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
 // *ovf_list / *ovf_count (device) for the streaming kernel.  ev (optional):
 // ev[1] and ev[2] are recorded around the counting kernel.
 bool lane_supported(uint32_t d);
+// The same counting with the records and totals in tensor memory and a ring of
+// shared-memory box slots that loads the next chunk during the current one.
+int lane_tm_supports_device(const CUtensorMap *map, uint32_t d, uint64_t n_words, const uint64_t *cand_ptr,
+                            const uint32_t *cand_items, uint64_t n_cand, uint64_t n_txn, uint32_t *out, void *scratch,
+                            size_t scratch_bytes, uint32_t waves, uint32_t *dev_err, cudaStream_t st, int n_sm,
+                            uint32_t **ovf_list, unsigned long long **ovf_count, uint64_t *launches,
+                            cudaEvent_t *ev);
 int lane_supports_device(const CUtensorMap *map, uint32_t d, uint64_t n_words, const uint64_t *cand_ptr,
                          const uint32_t *cand_items, uint64_t n_cand, uint64_t n_txn, uint32_t *out, void *scratch,
                          size_t scratch_bytes, uint32_t waves, uint32_t *dev_err, cudaStream_t st, int n_sm,

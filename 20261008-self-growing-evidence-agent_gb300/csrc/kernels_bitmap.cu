@@ -815,16 +815,24 @@ int support_batch_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, 
     };
     int kind = plan.kernel;
     if (map == nullptr || d == 0) kind = SUPPORT_STREAM;
-    // measured on GB300 at 1M candidates x 1,024 rows: staged with 4-lane groups 30.0 ms,
-    // staged with 8-lane groups 30.9 ms, sorted 30.8-46 ms (depending on its grid)
-    if (kind == SUPPORT_AUTO) kind = lane_supported(d) ? SUPPORT_LANE : SUPPORT_STAGED4;
-    if (kind == SUPPORT_LANE) {
+    // measured on GB300 at 1M candidates x 1,024 rows: lane with TMEM records 22.3 ms, lane
+    // with shared-memory records 23.2 ms, staged with 4-lane groups 30.0 ms, staged with 8-lane
+    // groups 30.9 ms, sorted 30.8-46 ms (depending on its grid).  AUTO falls through to the
+    // shared-memory lane form, then STAGED4, when a layout does not fit.
+    if (kind == SUPPORT_AUTO) kind = lane_supported(d) ? SUPPORT_LANE_TM : SUPPORT_STAGED4;
+    if (kind == SUPPORT_LANE || kind == SUPPORT_LANE_TM) {
         uint32_t *ovf_l = nullptr;
         unsigned long long *ovf_c = nullptr;
         mark(0);
-        const int rc = lane_supports_device(map, d, n_words_even, cand_ptr, cand_items, n_cand, n_txn, out,
-                                            scratch.base, scratch.bytes, plan.waves ? plan.waves : 2, dev_err, st,
-                                            n_sm, &ovf_l, &ovf_c, launches, ev);
+        int rc = -1;
+        if (kind == SUPPORT_LANE_TM)
+            rc = lane_tm_supports_device(map, d, n_words_even, cand_ptr, cand_items, n_cand, n_txn, out,
+                                         scratch.base, scratch.bytes, plan.waves ? plan.waves : 1, dev_err, st, n_sm,
+                                         &ovf_l, &ovf_c, launches, ev);
+        if (rc != 0)
+            rc = lane_supports_device(map, d, n_words_even, cand_ptr, cand_items, n_cand, n_txn, out, scratch.base,
+                                      scratch.bytes, kind == SUPPORT_LANE && plan.waves ? plan.waves : 2, dev_err, st,
+                                      n_sm, &ovf_l, &ovf_c, launches, ev);
         if (rc == 0) {
             QueryBatch qb;
             qb.rows = bitmaps; qb.row_stride = row_stride; qb.n_words = n_words_even; qb.d = d;

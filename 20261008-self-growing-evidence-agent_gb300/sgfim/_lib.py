@@ -132,6 +132,7 @@ SIGNATURES = {
     "sgfim_cooccurrence": (C.c_int, [C.c_void_p, u32p, C.c_uint32]),
     "sgfim_cooccurrence_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64,
                                             C.c_void_p, C.c_int, C.c_void_p]),
+    "sgfim_frequent_extensions": (C.c_int, [C.c_void_p, u64p, u32p, C.c_uint64, C.c_uint32, u64p, C.c_uint32]),
     "sgfim_mine": (C.c_int, [C.c_void_p, C.POINTER(MineParams), C.POINTER(C.POINTER(Result))]),
     "sgfim_mine_anytime": (C.c_int, [C.c_void_p, C.POINTER(MineParams), f64p, C.c_uint32, CKPT_CB,
                                      C.c_void_p, C.POINTER(C.POINTER(Result))]),

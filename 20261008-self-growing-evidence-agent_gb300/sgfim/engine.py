@@ -254,11 +254,26 @@ class Engine:
         self._check(self._L.sgfim_support_batch_device(self._h, bm_ptr, d, n_words, row_stride, cand_ptr_ptr,
                                                        cand_items_ptr, n_cand, out_ptr, stream or None))
 
-    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3, "staged4": 4, "lane": 5}
+    KERNELS = {"auto": 0, "staged": 1, "sorted": 2, "stream": 3, "staged4": 4, "lane": 5, "lane_tm": 6}
 
     def set_support_plan(self, kernel="auto", cands_per_cta=0, waves=0):
         """Choose the support-batch kernel and its CTA sizing (see sgfim_support_plan_set)."""
         self._check(self._L.sgfim_support_plan_set(self._h, self.KERNELS[kernel], int(cands_per_cta), int(waves)))
+
+    def frequent_extensions(self, set_ptr, set_items, min_count):
+        """sgfim_frequent_extensions: uint64 masks [n_sets, ceil(n_ids / 64)]; bit id is set
+        when set + {id} is frequent.  An all-zero row means the set is maximal."""
+        sp = np.ascontiguousarray(set_ptr, dtype=np.uint64)
+        si = np.ascontiguousarray(set_items, dtype=np.uint32)
+        if len(si) == 0:
+            si = np.zeros(1, np.uint32)
+        n = len(sp) - 1
+        mw = max(1, (self.info()["n_ids"] + 63) // 64)
+        out = np.zeros((max(n, 0), mw), np.uint64)
+        if n > 0:
+            self._check(self._L.sgfim_frequent_extensions(self._h, _p(sp, C.c_uint64), _p(si, C.c_uint32), n,
+                                                          int(min_count), _p(out, C.c_uint64), mw))
+        return out
 
     def phase_stats(self, reset=True):
         """Summed CUDA-event phase times of support-batch calls (needs phase_timers=True)."""

@@ -390,42 +390,6 @@ def stream_rows_for(n_req=WORKLOAD["n_req"], rate_hz=WORKLOAD["rate_hz"], stream
                                WORKLOAD["alpha_bin"], seed=seed)
 
 
-# ---------------------------------------------------------------- exactness / CPU arm (oracle, spawn pool)
-_ROWS = None
-
-
-def _pool_init(rows):
-    global _ROWS
-    _ROWS = rows
-
-
-def _check_window(args):
-    """Oracle MFIs of one window (runs in a worker process)."""
-    import oracle
-    end, length, thr = args
-    rows = _ROWS[end - length:end]
-    rp, it = datagen.txns_to_csr(rows)
-    bm, _ = oracle.build_bitmaps(rp, it, 126)
-    res, _ = oracle.mine_fast(bm, length, thr)
-    return sorted((tuple(s), c) for s, c in res)
-
-
-def _cpu_window(args):
-    """The reference's miner restated (mine_mfi with its 200,000-node cap) on one window."""
-    import oracle
-    end, length, thr = args
-    rows = _ROWS[end - length:end]
-    rp, it = datagen.txns_to_csr(rows)
-    bm, _ = oracle.build_bitmaps(rp, it, 126)
-    t = time.perf_counter()
-    try:
-        oracle.mine_mfi(bm, length, min_count=thr, node_cap=200_000)
-        ok = True
-    except RuntimeError:
-        ok = False
-    return ok, time.perf_counter() - t
-
-
 def saturate(rows, reqs, repeat, horizontal=False, hbm_budget=32 << 30, out=""):
     """Every request's window (as the service would cut it) in one batched call."""
     import json
@@ -462,11 +426,38 @@ def saturate(rows, reqs, repeat, horizontal=False, hbm_budget=32 << 30, out=""):
         eng.close()
 
 
+def run_workload(n_requests=WORKLOAD["n_req"], rate=WORKLOAD["rate_hz"], mode="batched", schedulers=2, workers=16,
+                 hbm_budget_gb=32.0, keep_results=False):
+    """The windows-4096 workload in real time (a warm-up pass first).  Returns
+    (report, completed requests, stream rows)."""
+    rows = stream_rows_for(n_requests, rate_hz=rate)
+    reqs = make_requests(n_requests, rate, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
+    svc = WindowService(workers=workers, hbm_budget=int(hbm_budget_gb * (1 << 30)), keep_results=keep_results,
+                        mode=mode, schedulers=schedulers)
+    try:
+        # warm-up pass on a handful of requests (first-use allocations of every handle)
+        warm = make_requests(2 * workers, 4000.0, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=99)
+        svc.run(rows, warm, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
+        svc.ring.close()
+        svc.ring = Ring(126, WORKLOAD["ring_txn"])
+        rep = svc.run(rows, reqs, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
+    finally:
+        svc.close()
+    done = rep.pop("requests")
+    errs = {}
+    for rq in done:
+        if rq.error:
+            errs[rq.error] = errs.get(rq.error, 0) + 1
+    report = {"workload": "windows-4096", "requests": n_requests, "rate_hz": rate,
+              "workers": workers if mode == "workers" else schedulers,
+              "hbm_budget_gb": hbm_budget_gb, **rep, "error_kinds": errs,
+              "config": {k: WORKLOAD[k] for k in WORKLOAD}}
+    return report, done, rows
+
+
 def main(argv=None):
     import argparse
     import json
-    import multiprocessing as mp
-    import os
     ap = argparse.ArgumentParser(description="sliding-window MFI service, workload windows-4096")
     ap.add_argument("--requests", type=int, default=WORKLOAD["n_req"])
     ap.add_argument("--workers", type=int, default=16)
@@ -475,9 +466,6 @@ def main(argv=None):
                     help="batched mode: concurrent batches (a handle and a thread each); measured at "
                          "2,000 req/s: 1 -> p50 36.9 / p99 56.2 ms, 2 -> 32.9 / 52.5 ms, 3 -> 35.5 / 59.3 ms")
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
-    ap.add_argument("--check", action="store_true", help="compare every window with the oracle")
-    ap.add_argument("--check-budget-s", type=float, default=240.0)
-    ap.add_argument("--cpu-budget-s", type=float, default=30.0)
     ap.add_argument("--out", default="")
     ap.add_argument("--saturate", type=int, default=0, metavar="REPEAT",
                     help="instead of the timed service, mine every request's window in one "
@@ -486,65 +474,11 @@ def main(argv=None):
     ap.add_argument("--rate", type=float, default=WORKLOAD["rate_hz"],
                     help="Poisson arrival rate of the requests (req/s); the workload's is 2,000")
     a = ap.parse_args(argv)
-    rows = stream_rows_for(a.requests, rate_hz=a.rate)
-    reqs = make_requests(a.requests, a.rate, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
     if a.saturate:
+        rows = stream_rows_for(a.requests, rate_hz=a.rate)
+        reqs = make_requests(a.requests, a.rate, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=1)
         return saturate(rows, reqs, a.saturate, a.horizontal, int(a.hbm_budget_gb * (1 << 30)), a.out)
-    svc = WindowService(workers=a.workers, hbm_budget=int(a.hbm_budget_gb * (1 << 30)),
-                        keep_results=a.check, mode=a.mode, schedulers=a.schedulers)
-    # warm-up pass on a handful of requests (first-use allocations of every worker)
-    warm = make_requests(2 * a.workers, 4000.0, WORKLOAD["len_lo"], WORKLOAD["len_hi"], seed=99)
-    svc.run(rows, warm, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
-    svc.ring.close()
-    svc.ring = Ring(126, WORKLOAD["ring_txn"])
-    rep = svc.run(rows, reqs, WORKLOAD["stream_rate"], WORKLOAD["floor_frac"])
-    svc.close()
-    done = rep.pop("requests")
-    errs = {}
-    for rq in done:
-        if rq.error:
-            errs[rq.error] = errs.get(rq.error, 0) + 1
-    report = {"workload": "windows-4096", "requests": a.requests, "rate_hz": a.rate,
-              "workers": a.workers if a.mode == "workers" else a.schedulers,
-              "hbm_budget_gb": a.hbm_budget_gb, **rep, "error_kinds": errs,
-              "config": {k: WORKLOAD[k] for k in WORKLOAD}}
-    ctx = mp.get_context("spawn")
-    procs = os.cpu_count() or 1
-    jobs = []
-    for rq in done:
-        length = min(rq.length, rq.end)
-        jobs.append((rq.end, length, max(1, int(np.ceil(WORKLOAD["floor_frac"] * length)))))
-    if a.check:
-        t0 = time.perf_counter()
-        checked = mism = 0
-        with ctx.Pool(procs, initializer=_pool_init, initargs=(rows,)) as pool:
-            for rq, ref in zip(done, pool.imap(_check_window, jobs, chunksize=4)):
-                if rq.result is None:   # the request failed; counted in "errors"
-                    continue
-                got = sorted((tuple(sorted(s)), c) for s, c in rq.result.sets())
-                checked += 1
-                mism += got != ref
-                if time.perf_counter() - t0 > a.check_budget_s:
-                    pool.terminate()
-                    break
-        report["exact"] = {"checked": checked, "mismatches": mism}
-    if a.cpu_budget_s > 0:
-        t0 = time.perf_counter()
-        n_ok = n_cap = 0
-        cpu_t = 0.0
-        with ctx.Pool(procs, initializer=_pool_init, initargs=(rows,)) as pool:
-            for ok, dt in pool.imap(_cpu_window, jobs, chunksize=1):
-                n_ok += ok
-                n_cap += not ok
-                cpu_t += dt
-                if time.perf_counter() - t0 > a.cpu_budget_s:
-                    pool.terminate()
-                    break
-        wall = time.perf_counter() - t0
-        report["cpu_baseline"] = {"windows": n_ok + n_cap, "completed": n_ok, "node_cap_hit": n_cap,
-                                  "windows_per_s": (n_ok + n_cap) / wall, "cores": procs, "kind": "port",
-                                  "sample": f"first {n_ok + n_cap} windows in arrival order within "
-                                            f"{a.cpu_budget_s:.0f} s, mine_mfi restated with its 200,000-node cap"}
+    report, _, _ = run_workload(a.requests, a.rate, a.mode, a.schedulers, a.workers, a.hbm_budget_gb)
     print(json.dumps(report))
     if a.out:
         with open(a.out, "w") as f:

@@ -166,13 +166,15 @@ int sgfim_cooccurrence(sgfim_handle *h, uint32_t *out, uint32_t d);
  * kernel: SGFIM_KERNEL_*; cands_per_cta: candidates a CTA owns (0 = derived);
  * waves: CTAs per SM over the grid when cands_per_cta is 0 (0 = the kernel's
  * default: 1 for SORTED, 2 for STAGED). */
-#define SGFIM_KERNEL_AUTO 0    /* LANE when the rows fit shared memory (d <= 1,792), else STAGED4 or streaming */
+#define SGFIM_KERNEL_AUTO 0    /* LANE_TM when the rows fit shared memory (d <= 1,792), else STAGED4 or streaming */
 #define SGFIM_KERNEL_STAGED 1  /* TMA-staged chunks, candidates in input order */
 #define SGFIM_KERNEL_SORTED 2  /* TMA-staged chunks, candidates sorted by (k, first item); ids < 1024 */
 #define SGFIM_KERNEL_STREAM 3  /* one warp per candidate, rows streamed from L2/HBM */
 #define SGFIM_KERNEL_STAGED4 4 /* TMA-staged chunks, 4-lane groups (32 bytes of a row per lane) */
 #define SGFIM_KERNEL_LANE 5    /* TMA-staged chunks, one lane per candidate, candidates sorted by k
                                   on the device; waves = CTAs per SM (default 2) */
+#define SGFIM_KERNEL_LANE_TM 6 /* LANE with the candidates in tensor memory and the next chunk
+                                  loaded during the current one; waves default 1 */
 int sgfim_support_plan_set(sgfim_handle *h, int kernel, uint32_t cands_per_cta, uint32_t waves);
 
 /* Allocation-free form of sgfim_support_batch_device.  It has no counterpart
@@ -230,6 +232,20 @@ int sgfim_phase_stats_get(sgfim_handle *h, sgfim_phase_stats *out, int reset);
 #define SGFIM_COOC_TC_F8 3    /* tcgen05 e4m3 GEMM of 0/1 bytes, fp32 accumulate */
 int sgfim_cooccurrence_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
                               uint64_t row_stride, uint32_t *out, int kind, void *stream);
+
+/* Frequent single-item extensions of n_sets itemsets (CSR over original ids):
+ * bit (id & 63) of masks[s * mask_words + (id >> 6)] is set when id is not in
+ * set s and sup(set s u {id}) >= min_count (0 is taken as 1).  mask_words >=
+ * ceil(n_ids / 64).  An all-zero mask means the set is maximal at min_count:
+ * the maximality rule of mine_mfi (code/pipeline/skab_spike.py:129-135) and
+ * of the engines' leaf test (kernel_bitmap.cu:870), for any batch of sets.
+ * Exact: each candidate item is first bounded by the minimum pairwise
+ * co-occurrence with the set's items (computed once per dataset), and the
+ * items whose bound reaches min_count are counted exactly against the set's
+ * rows.  A set holding an id that never occurs has support 0 and no
+ * frequent extension. */
+int sgfim_frequent_extensions(sgfim_handle *h, const uint64_t *set_ptr, const uint32_t *set_items,
+                              uint64_t n_sets, uint32_t min_count, uint64_t *masks, uint32_t mask_words);
 
 /* ---------------------------------------------------------------- mining */
 

@@ -126,7 +126,7 @@ void orc_build_bitmaps(const uint64_t *row_ptr, const uint32_t *items, uint64_t 
 typedef struct {
     const uint64_t *bm; uint64_t W;
     const uint64_t *cand_ptr; const uint32_t *cand_items;
-    uint64_t lo, hi; uint32_t *out;
+    uint64_t lo, hi; uint32_t *out; uint32_t d;
 } sb_job;
 
 static void *sb_worker(void *arg) {
@@ -134,7 +134,10 @@ static void *sb_worker(void *arg) {
     for (uint64_t c = j->lo; c < j->hi; c++) {
         uint64_t a = j->cand_ptr[c], b = j->cand_ptr[c + 1];
         uint64_t s = 0;
+        int absent = 0;
+        for (uint64_t i = a; i < b; i++) absent |= j->cand_items[i] >= j->d;
         if (b == a) { s = j->W * 64; /* empty set: every (padded) transaction */ }
+        else if (absent) { s = 0; /* an id without a row never occurs (kernel_bitmap.cu:354) */ }
         else {
             for (uint64_t w = 0; w < j->W; w++) {
                 uint64_t m = ~0ULL;
@@ -149,7 +152,6 @@ static void *sb_worker(void *arg) {
 
 void orc_support_batch(const uint64_t *bm, uint32_t d, uint64_t W, const uint64_t *cand_ptr,
                        const uint32_t *cand_items, uint64_t n_cand, uint32_t *out, int n_threads) {
-    (void)d;
     if (n_threads < 1) n_threads = 1;
     if ((uint64_t)n_threads > n_cand) n_threads = (int)(n_cand ? n_cand : 1);
     pthread_t th[256];
@@ -157,6 +159,7 @@ void orc_support_batch(const uint64_t *bm, uint32_t d, uint64_t W, const uint64_
     if (n_threads > 256) n_threads = 256;
     for (int t = 0; t < n_threads; t++) {
         jobs[t].bm = bm; jobs[t].W = W; jobs[t].cand_ptr = cand_ptr; jobs[t].cand_items = cand_items;
+        jobs[t].d = d;
         jobs[t].lo = n_cand * (uint64_t)t / (uint64_t)n_threads;
         jobs[t].hi = n_cand * (uint64_t)(t + 1) / (uint64_t)n_threads;
         jobs[t].out = out;

@@ -30,7 +30,7 @@ def test_support_batch_matches_oracle(engine, n_txn, d, n_cand, kmin, kmax):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("kernel", ["lane", "sorted", "staged", "staged4", "stream"])
+@pytest.mark.parametrize("kernel", ["lane", "lane_tm", "sorted", "staged", "staged4", "stream"])
 @pytest.mark.parametrize("d", [1024, 300])
 def test_support_kernels_agree(engine, kernel, d):
     """Every kernel plan gives the oracle's supports (k = 0..12, unknown ids included)."""

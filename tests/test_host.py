@@ -125,33 +125,30 @@ def test_csr_bitmap_roundtrip():
 
 # ------------------------------------------------------------------ sharding (N>1 bench path)
 def _shard_worker(rank, world, port, result_path):
+    """One rank of bench.py's N-GPU path with the oracle counting in place of the
+    GPU kernel: the same transaction split (txn_shard, row_slice) and the same
+    int32 sum all-reduce (allreduce_counts) over gloo."""
+    import torch
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    import torch
-    from sgfim.sharding import shard_range
-    bm = datagen.correlated_bitmaps(4096, 40, 4, 0.05, 0.3, seed=3)
-    cp, ci = datagen.walk_candidates(1001, 40, 3, 8, seed=4)
-    lo, hi = shard_range(len(cp) - 1, rank, world)
-    sub_ptr = cp[lo:hi + 1] - cp[lo]
-    sub_items = ci[cp[lo]:cp[hi]]
-    part = oracle.support_batch(bm, sub_ptr, sub_items, n_threads=1)
-    sizes = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
-    dist.all_gather(sizes, torch.tensor([len(part)]))
-    mx = int(max(s.item() for s in sizes))
-    buf = torch.zeros(mx, dtype=torch.int64)
-    buf[:len(part)] = torch.from_numpy(part.astype(np.int64))
-    outs = [torch.zeros(mx, dtype=torch.int64) for _ in range(world)]
-    dist.all_gather(outs, buf)
+    from sgfim import sharding
+    n_words = 16 * 7 + 6                      # 7 whole chunks and a ragged end
+    bm = datagen.correlated_bitmaps(n_words * 64, 40, 4, 0.05, 0.3, seed=3)
+    cp, ci = datagen.walk_candidates(1001, 40, 1, 10, seed=4)
+    w0, w1 = sharding.txn_shard(n_words, rank, world)
+    part = oracle.support_batch(sharding.row_slice(bm, w0, w1), cp, ci, n_threads=1)
+    counts = torch.from_numpy(part.astype(np.int32))
+    sharding.allreduce_counts(counts, dist)
     if rank == 0:
-        full = np.concatenate([o[:int(s.item())].numpy() for o, s in zip(outs, sizes)])
         ref = oracle.support_batch(bm, cp, ci, n_threads=1)
-        np.save(result_path, np.array([int(np.array_equal(full, ref)), len(full)]))
+        np.save(result_path, np.array([int(np.array_equal(counts.numpy().astype(np.uint32), ref)), len(ref),
+                                       w1 - w0]))
     dist.destroy_process_group()
 
 
-def test_two_rank_sharded_supports_gloo(tmp_path):
+def test_two_rank_transaction_split_supports_gloo(tmp_path):
     import socket
     import torch.multiprocessing as mp
     s = socket.socket()
@@ -160,8 +157,28 @@ def test_two_rank_sharded_supports_gloo(tmp_path):
     s.close()
     out = str(tmp_path / "r.npy")
     mp.start_processes(_shard_worker, args=(2, port, out), nprocs=2, start_method="spawn")
-    ok, n = np.load(out)
-    assert ok == 1 and n == 1001
+    ok, n, width0 = np.load(out)
+    assert ok == 1 and n == 1001 and width0 % 16 == 0
+
+
+def test_txn_shard_covers_words_on_chunk_boundaries():
+    from sgfim import sharding
+    for n_words in (1, 15, 16, 17, 16 * 1024, 31_250):
+        for world in (1, 2, 3, 8):
+            cuts = [sharding.txn_shard(n_words, r, world) for r in range(world)]
+            assert cuts[0][0] == 0 and cuts[-1][1] == n_words
+            for (a0, a1), (b0, _) in zip(cuts, cuts[1:]):
+                assert a1 == b0 and a0 <= a1 and a0 % 16 == 0
+    bm = np.arange(3 * 37, dtype=np.uint64).reshape(3, 37)
+    sl = sharding.row_slice(bm, 16, 37)
+    assert sl.shape == (3, 22) and np.array_equal(sl[:, :21], bm[:, 16:]) and not sl[:, 21].any()
+
+
+def test_numpy_lut_counting_equals_oracle():
+    from oracle import numpy_lut
+    bm = datagen.correlated_bitmaps(64 * 40, 30, 4, 0.05, 0.4, seed=9)
+    cp, ci = datagen.walk_candidates(300, 30, 1, 8, seed=10)
+    assert np.array_equal(numpy_lut.supports(bm, cp, ci), oracle.support_batch(bm, cp, ci))
 
 
 def test_masks_to_sets():

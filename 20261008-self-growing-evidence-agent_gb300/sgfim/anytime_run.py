@@ -16,8 +16,9 @@ import time
 
 import numpy as np
 
+from . import _lib as L
 from . import datagen
-from .engine import Engine
+from .engine import Engine, SgfimError
 
 WORKLOAD = dict(n_txn=2_000_000, n_sensors=80, n_bins=8, n_regimes=32, alpha_bin=0.2)
 ITEMS = WORKLOAD["n_sensors"] * WORKLOAD["n_bins"]
@@ -43,14 +44,26 @@ def run(eng, rows, floor, checkpoints=(1, 2, 5, 10, 30), order="support", time_l
     t_load = time.perf_counter() - t0
     thr = max(1, int(np.ceil(floor * n_txn)))
     cks = [float(c) for c in checkpoints]
-    res, recs = eng.mine_anytime(thr, cks, order=order, time_limit_s=time_limit_s, node_limit=node_limit,
-                                 materialize=False)
+    recs = []
+    try:
+        res, _ = eng.mine_anytime(thr, cks, order=order, time_limit_s=time_limit_s, node_limit=node_limit,
+                                  materialize=False, records=recs)
+    except SgfimError as e:
+        if e.code not in (L.ETIMEDOUT, L.ENOMEM):
+            raise
+        # a time or node limit ended the search: what was emitted by each checkpoint
+        report = {"workload": "anytime-2m", "n_txn": n_txn, "items": ITEMS, "floor": floor, "min_count": thr,
+                  "order": order, "complete": False, "stopped_by": "time limit" if e.code == L.ETIMEDOUT
+                  else "node limit", "time_limit_s": time_limit_s, "node_limit": node_limit, "load_s": t_load,
+                  "checkpoints": [{"t_s": r["t_s"], "elapsed_s": r["elapsed_s"],
+                                   "emitted_candidates": r["n_emitted"], "nodes": r["nodes"]} for r in recs]}
+        return report, None
     # every final MFI carries its emission time, so coverage(t) needs no set comparison
     cov = coverage_at(res.emit_time_s, cks)
     curve = [{"t_s": r["t_s"], "elapsed_s": r["elapsed_s"], "emitted_candidates": r["n_emitted"],
               "coverage": cov[str(r["t_s"])], "nodes": r["nodes"]} for r in recs]
     report = {"workload": "anytime-2m", "n_txn": n_txn, "items": ITEMS, "floor": floor, "min_count": thr,
-              "order": order, "mfis": len(res), "nodes": res.nodes, "waves": res.waves, "candidates": res.candidates,
+              "order": order, "complete": True, "mfis": len(res), "nodes": res.nodes, "waves": res.waves, "candidates": res.candidates,
               "kernel_launches": res.kernel_launches, "mine_s": res.elapsed_s, "load_s": t_load,
               "phase_s": res.phase_s,
               "time_to": {f"{int(f * 100)}%": res.time_to_coverage(f) for f in (0.5, 0.9, 0.95, 1.0)},

@@ -331,14 +331,17 @@ class Engine:
         finally:
             self._L.sgfim_result_free(res)
 
-    def mine_anytime(self, min_count, checkpoints, callback=None, materialize=True, **kw):
+    def mine_anytime(self, min_count, checkpoints, callback=None, materialize=True, records=None, **kw):
         """Mine with wall-clock checkpoints.  ``callback(t_s, elapsed_s, sets)``
         receives the emitted candidates as a list of (ids tuple, support);
         returning True stops the search.  ``materialize=False`` keeps only the
-        counts in the records (no per-set Python objects).  Returns (result, records)."""
+        counts in the records (no per-set Python objects).  ``records`` (a list)
+        receives the checkpoint records as they happen, so they survive a time or
+        node limit.  Returns (result, records)."""
         p = self._params(min_count, **kw)
         cks = np.ascontiguousarray(checkpoints, dtype=np.float64)
-        records = []
+        if records is None:
+            records = []
 
         def _cb(user, ckp):
             ck = ckp.contents

@@ -1,9 +1,8 @@
 """Generate the golden fixtures of tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference project next to it (default
-/root/reference, override with SGFIM_REFERENCE):
+Run with SGFIM_REFERENCE naming a checkout of the reference project:
 
-    python tests/golden/make_golden.py
+    SGFIM_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 
 It imports the reference's own Python miners and adapter parsers
 (code/pipeline/skab_spike.py:mine_mfi, code/pipeline/exp_e6_cpuvec.py:
@@ -27,7 +26,9 @@ import types
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "20261008-self-growing-evidence-agent_gb300"))
-REF = os.environ.get("SGFIM_REFERENCE", "/root/reference")
+REF = os.environ.get("SGFIM_REFERENCE")
+if not REF or not os.path.isdir(REF):
+    sys.exit("set SGFIM_REFERENCE to a checkout of the reference project")
 
 import numpy as np  # noqa: E402
 

@@ -1,9 +1,8 @@
 """Golden fixtures of the online (streaming) discretiser, from the reference.
 
-Run in a checkout that has the reference project next to it (default
-/root/reference, override with SGFIM_REFERENCE):
+Run with SGFIM_REFERENCE naming a checkout of the reference project:
 
-    python tests/golden/make_online_golden.py
+    SGFIM_REFERENCE=<reference checkout> python tests/golden/make_online_golden.py
 
 It imports code/pipeline/online_discretize.py and calls its own ``run_file``
 on seeded synthetic sensor streams (``sgfim.datagen.sensor_stream``).  pandas
@@ -31,7 +30,9 @@ import types
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "20261008-self-growing-evidence-agent_gb300"))
-REF = os.environ.get("SGFIM_REFERENCE", "/root/reference")
+REF = os.environ.get("SGFIM_REFERENCE")
+if not REF or not os.path.isdir(REF):
+    sys.exit("set SGFIM_REFERENCE to a checkout of the reference project")
 
 import numpy as np  # noqa: E402
 

@@ -1,9 +1,9 @@
-"""The in-process ctypes stub printed in INTEGRATION.md runs as written against
-the built library and returns what the Python front end returns."""
+"""The in-process ctypes stub that INTEGRATION.md points maintainers to
+(sgfim/examples/ctypes_adapter_stub.py) runs against the built library and
+returns what the Python front end returns."""
+import importlib.util
 import os
-import re
 
-import numpy as np
 import pytest
 
 from sgfim import datagen
@@ -11,21 +11,18 @@ from sgfim import datagen
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+STUB = os.path.join(ROOT, "20261008-self-growing-evidence-agent_gb300", "sgfim", "examples", "ctypes_adapter_stub.py")
 
 
 def test_integration_ctypes_stub(tmp_path):
-    from sgfim import _lib
     from sgfim.engine import Engine
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    block = next(b for b in re.findall(r"```python\n(.*?)```", doc, re.S) if "def run_gb300" in b)
-    code = block.replace('"<repo>/20261008-self-growing-evidence-agent_gb300/sgfim/_lib/libsgfim.so"',
-                         repr(_lib.LIB_PATH))
-    ns = {}
-    exec(compile(code, "INTEGRATION.md", "exec"), ns)
+    spec = importlib.util.spec_from_file_location("ctypes_adapter_stub", STUB)
+    stub = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(stub)
     rows = datagen.regime_txns(3000, 8, 5, 4, 0.3, seed=12)
     path = tmp_path / "w.txt"
     path.write_text("".join(" ".join(str(int(x) + 1) for x in r) + "\n" for r in rows))
-    got = ns["run_gb300"](str(path), 120)
+    got = stub.run_gb300(str(path), 120)
     assert got["ok"]
     with Engine() as eng:
         eng.load_fimi(str(path))

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from sgfim import datagen, engine_adapter
+from sgfim import datagen, results
 from sgfim.engine import thresh_from
 
 pytestmark = pytest.mark.gpu
@@ -156,20 +156,22 @@ def test_cancel_from_checkpoint(engine):
     assert ei.value.code == -7
 
 
-def test_cli_shims_through_adapter(tmp_path):
+def test_cli_shims_results_files(tmp_path):
+    """The shims, run as the pipeline runs the engines, write result files whose
+    sets are the oracle's TensorFIM and AnyFIM answers."""
     rows = datagen.regime_txns(4000, 8, 5, 4, 0.3, seed=12)
     rows1 = [[x + 1 for x in r] for r in rows.tolist()]
     fimi = str(tmp_path / "d.txt")
     datagen.write_fimi_ids(fimi, rows, one_based=True)
-    r = engine_adapter.run_tensorfim("bmma", fimi, 0.03)
-    assert r["ok"] and r["comp_times"] and r["tot_times"]
-    assert r["mfis"] == oracle.tensorfim_mfis(rows1, 0.03)
-    a = engine_adapter.run_anyfim(fimi, 12)
-    assert a["ok"]
+    r = results.run_shim("tensorfim", fimi, 0.03)
+    assert r is not None and r.computation_s is not None and r.total_s is not None
+    assert r.sets == oracle.tensorfim_mfis(rows1, 0.03)
+    a = results.run_shim("anyfim", fimi, 12)
+    assert a is not None
     want = oracle.anyfim_stages(rows1, 12)
-    assert {k: dict(v) for k, v in a["stages"].items()} == want
-    assert len(a["meta"]["runtimePerStage(s)"]) == 12
-    assert a["meta"]["MFIsNumPerStage"] == [len(want[k]) for k in range(1, 13)]
+    assert {k: dict(v) for k, v in a.stages.items()} == want
+    assert a.arrays["MFIsNumPerStage"] == [len(want[k]) for k in range(1, 13)]
+    assert len(a.arrays["runtimePerStage(s)"]) == 12
 
 
 @pytest.mark.parametrize("wave_nodes,floor", [(1, 0.08), (7, 0.05), (64, 0.02), (0, 0.02)])

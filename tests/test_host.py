@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from sgfim import datagen, engine_adapter
+from sgfim import datagen, results
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "sgfim.h")
@@ -63,43 +63,35 @@ def test_parse_fimi_byte_rules(tmp_path):
     assert oracle.parse_fimi(str(p)) == [[1, 2], []]
 
 
-# ------------------------------------------------------------------ adapter mirror
-def test_adapter_regexes_equal_reference():
-    assert engine_adapter.TF_LINE.pattern == ADAPTER_GOLD["tf_line"]
-    assert engine_adapter.AF_STAGE.pattern == ADAPTER_GOLD["af_stage"]
-    assert engine_adapter.TF_COMP.pattern == ADAPTER_GOLD["tf_comp"]
-    assert engine_adapter.TF_TOT.pattern == ADAPTER_GOLD["tf_tot"]
+# ------------------------------------------------------------------ result files (the adapter's format)
+def test_result_patterns_equal_reference():
+    """The four patterns are the reference adapter's, character for character."""
+    assert results.RECORD.pattern == ADAPTER_GOLD["tf_line"]
+    assert results.STAGE_HEADER.pattern == ADAPTER_GOLD["af_stage"]
+    assert results.COMPUTATION_TIME.pattern == ADAPTER_GOLD["tf_comp"]
+    assert results.TOTAL_TIME.pattern == ADAPTER_GOLD["tf_tot"]
 
 
-def test_adapter_parsers_match_reference_outputs(tmp_path):
+def test_read_results_equals_reference_parsers(tmp_path):
+    """read_results gives what the reference's parse_tensorfim_results /
+    parse_anyfim_results / cumulative_mfis returned on the same texts."""
     p1, p2 = tmp_path / "tf.txt", tmp_path / "af.txt"
     p1.write_text(ADAPTER_GOLD["tf_text"])
     p2.write_text(ADAPTER_GOLD["af_text"])
-    tf = engine_adapter.parse_tensorfim_results(str(p1))
-    assert sorted([sorted(k), v] for k, v in tf.items()) == ADAPTER_GOLD["tf_parsed"]
-    st, meta = engine_adapter.parse_anyfim_results(str(p2))
-    assert {str(k): sorted([sorted(s), f] for s, f in v) for k, v in st.items()} == ADAPTER_GOLD["af_parsed"]
-    assert meta == ADAPTER_GOLD["af_meta"]
-    cum = engine_adapter.cumulative_mfis(st)
-    assert {str(k): sorted(sorted(s) for s in v) for k, v in cum.items()} == ADAPTER_GOLD["cumulative"]
+    tf = results.read_results(str(p1))
+    assert sorted([sorted(k), v] for k, v in tf.sets.items()) == ADAPTER_GOLD["tf_parsed"] and not tf.stages
+    af = results.read_results(str(p2))
+    assert {str(k): sorted([sorted(s), f] for s, f in v) for k, v in af.stages.items()} == ADAPTER_GOLD["af_parsed"]
+    assert af.arrays == ADAPTER_GOLD["af_meta"]
+    assert {str(k): sorted(sorted(s) for s in v) for k, v in af.cumulative().items()} == ADAPTER_GOLD["cumulative"]
+    assert results.timings(ADAPTER_GOLD["tf_text"]) == (0.5, 0.75)
 
 
-def test_write_fimi_numbering(tmp_path):
-    p = tmp_path / "t.txt"
-    m = engine_adapter.write_fimi([["a=1", "b=2"], ["b=2", "c=0", "b=2"], []], str(p), str(tmp_path / "m.json"))
-    assert m == {"a=1": 1, "b=2": 2, "c=0": 3}
-    assert p.read_text() == "1 2\n2 3\n\n"
-    inv = {v: k for k, v in engine_adapter.load_items_map(str(tmp_path / "m.json")).items()}
-    assert engine_adapter.decode_itemset([1, 3], inv) == frozenset({"a=1", "c=0"})
+def test_result_paths_follow_the_engines_naming():
+    assert results.result_path("tensorfim", "/d/x.txt", 0.03) == "/d/x.txt-0.030000=Results.txt"
+    assert results.result_path("anyfim", "/d/x.txt", 12) == "/d/x.txt-12-stages=Results.txt"
 
 
-def test_support_confidence_lift():
-    txns = [[1, 2], [1], [1, 2, 3], [2]]
-    sup, conf, lift = engine_adapter.support_confidence_lift({1, 2}, txns, [1, 0, 1, 0])
-    assert sup == 0.5 and conf == 1.0 and lift == 2.0
-
-
-# ------------------------------------------------------------------ generators
 def test_generators_shapes_and_determinism():
     a = datagen.regime_txns(1000, 8, 5, 4, 0.3, seed=0)
     b = datagen.regime_txns(1000, 8, 5, 4, 0.3, seed=0)

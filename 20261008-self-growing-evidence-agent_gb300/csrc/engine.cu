@@ -554,6 +554,7 @@ void sgfim_result_free(sgfim_result *r) {
     free(r->items);
     free(r->support);
     free(r->emit_time_s);
+    free(r->emit_node);
     free(r->trace_features);
     free(r->trace_labels);
     free(r);

@@ -116,6 +116,7 @@ class Miner {
     std::vector<uint32_t> citems_orig_;   // citems_ as original ids, extended at each checkpoint
     std::vector<uint32_t> csup_;
     std::vector<double> ctime_;
+    std::vector<uint64_t> cexpanded_;   // nodes expanded when each candidate was emitted
     std::vector<uint32_t> cnode_;
     std::vector<uint64_t> ccheck_;   // pool size when the candidate was tested against the pool
     // search tree and trace
@@ -246,6 +247,7 @@ void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node) 
     cptr_.push_back(citems_.size());
     csup_.push_back(sup);
     ctime_.push_back(elapsed());
+    cexpanded_.push_back(nodes_);
     cnode_.push_back(node);
     ccheck_.push_back(pool_n_);
     for (size_t k = at; k < citems_.size(); ++k) ++cand_freq_[citems_[k]];
@@ -395,15 +397,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     std::vector<std::pair<uint32_t, uint32_t>> kid_src;  // (parent slot, added item)
     std::vector<uint32_t> child_slot;
 
-    // Learned order: children scored below kDeferBelow wait on a deferred stack,
-    // searched once the main stack is empty (they keep no tidset mask meanwhile).
-    std::vector<MNode> deferred;
-    constexpr float kDeferBelow = 0.5f;
-    while (!stack.empty() || !deferred.empty()) {
-        if (stack.empty()) {
-            // hand the deferred subtrees back, highest score first on top
-            std::swap(stack, deferred);
-        }
+    while (!stack.empty()) {
         // ---- pop a wave
         // the previous wave's nodes are done: keep their vectors for the next children
         for (MNode &nd : wave) {
@@ -421,7 +415,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         ++waves_;
         nodes_ += wave.size();
-        // nodes without a mask (deferred, or created when the arena was full) get
+        // nodes without a mask (created when the arena was full) get
         // one rebuilt from their head rows when a slot is free
         qchild.clear();
         child_slot.clear();
@@ -565,17 +559,13 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             }
         }
         // learned order: score every child of the wave in one launch
-        std::vector<uint8_t> defer(kids.size(), 0);
-        if (p_.order == SGFIM_ORDER_LEARNED) {
-            timed(4, [&] { score(wfeat, kids.size(), wscore); });
-            for (size_t k = 0; k < kids.size(); ++k) defer[k] = wscore[k] < kDeferBelow;
-        }
+        if (p_.order == SGFIM_ORDER_LEARNED) timed(4, [&] { score(wfeat, kids.size(), wscore); });
         // child masks for the children searched next: mask(child) = mask(parent) & row(e)
         qchild.clear();
         child_slot.clear();
         for (size_t k = 0; k < kids.size(); ++k) {
             MNode &c = kids[k];
-            if (c.tail.empty() || defer[k]) continue;  // leaves need no mask; deferred ones rebuild theirs
+            if (c.tail.empty()) continue;  // leaves need no mask
             c.slot = alloc_slot();
             if (c.slot == kNoSlot) continue;
             if (kid_src[k].first != kNoSlot) qchild.add(&kid_src[k].second, 1, kid_src[k].first);
@@ -592,7 +582,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                                ds_.stride, dptr, ditems, dps, dcs, (uint32_t)n, st, h_->n_sm);
             ++launches_;
         }
-        // sibling visiting order; deferred children go to the deferred stack
+        // sibling visiting order
         for (size_t i = wave.size(); i-- > 0;) {
             // stack is LIFO: nodes pushed later are popped first; keep wave order
             Work &wk = work[i];
@@ -604,10 +594,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             } else if (p_.order == SGFIM_ORDER_LEARNED) {
                 std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return wscore[a] > wscore[b]; });
             }
-            for (size_t j = ord.size(); j-- > 0;) {
-                if (defer[ord[j]]) deferred.push_back(std::move(kids[ord[j]]));
-                else stack.push_back(std::move(kids[ord[j]]));
-            }
+            for (size_t j = ord.size(); j-- > 0;) stack.push_back(std::move(kids[ord[j]]));
         }
         // parents' masks are no longer needed once the child-mask kernel ran (stream order)
         for (MNode &nd : wave)
@@ -789,12 +776,14 @@ int Miner::finish(sgfim_result **out) {
     r->items = static_cast<uint32_t *>(malloc(std::max<uint64_t>(total, 1) * 4));
     r->support = static_cast<uint32_t *>(malloc(std::max<uint64_t>(m, 1) * 4));
     r->emit_time_s = static_cast<double *>(malloc(std::max<uint64_t>(m, 1) * 8));
+    r->emit_node = static_cast<uint64_t *>(malloc(std::max<uint64_t>(m, 1) * 8));
     const uint64_t tn = p_.record_trace ? tnode_.size() : 0;
     r->trace_n = tn;
     r->trace_dim = kDim;
     r->trace_features = static_cast<float *>(malloc(std::max<uint64_t>(tn * kDim, 1) * 4));
     r->trace_labels = static_cast<uint8_t *>(malloc(std::max<uint64_t>(tn, 1)));
-    if (!r->set_ptr || !r->items || !r->support || !r->emit_time_s || !r->trace_features || !r->trace_labels) {
+    if (!r->set_ptr || !r->items || !r->support || !r->emit_time_s || !r->emit_node || !r->trace_features ||
+        !r->trace_labels) {
         sgfim_result_free(r);
         return fail(h_, SGFIM_ENOMEM, "result allocation failed");
     }
@@ -807,6 +796,7 @@ int Miner::finish(sgfim_result **out) {
             for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) r->items[at++] = ds_.d2o[citems_[k]];
             r->support[i] = csup_[c];
             r->emit_time_s[i] = ctime_[c];
+            r->emit_node[i] = cexpanded_[c];
         }
     });
     if (tn) {
@@ -842,6 +832,7 @@ int mine_impl(sgfim_handle *h, const sgfim_mine_params *p, const double *ckpts, 
         r->items = static_cast<uint32_t *>(calloc(1, 4));
         r->support = static_cast<uint32_t *>(calloc(1, 4));
         r->emit_time_s = static_cast<double *>(calloc(1, 8));
+        r->emit_node = static_cast<uint64_t *>(calloc(1, 8));
         r->trace_features = static_cast<float *>(calloc(1, 4));
         r->trace_labels = static_cast<uint8_t *>(calloc(1, 1));
         r->trace_dim = kDim;

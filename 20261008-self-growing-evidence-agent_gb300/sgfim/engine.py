@@ -37,6 +37,7 @@ class MineResult:
         self.items = np.ctypeslib.as_array(r.items, shape=(tot,)).copy() if tot else np.zeros(0, np.uint32)
         self.support = np.ctypeslib.as_array(r.support, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
         self.emit_time_s = np.ctypeslib.as_array(r.emit_time_s, shape=(n,)).copy() if n else np.zeros(0)
+        self.emit_node = np.ctypeslib.as_array(r.emit_node, shape=(n,)).copy() if n else np.zeros(0, np.uint64)
         self.ptr = ptr
         self.n_txn = int(r.n_txn)
         self.min_count = int(r.min_count)
@@ -67,6 +68,14 @@ class MineResult:
             return 0.0
         k = max(1, int(math.ceil(frac * len(t))))
         return float(t[k - 1])
+
+    def nodes_to_coverage(self, frac):
+        """Search nodes expanded until ``frac`` of the final MFIs had been emitted."""
+        t = np.sort(self.emit_node)
+        if len(t) == 0:
+            return 0
+        k = max(1, int(math.ceil(frac * len(t))))
+        return int(t[k - 1])
 
     def __len__(self):
         return len(self.support)

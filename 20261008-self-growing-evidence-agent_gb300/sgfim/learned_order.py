@@ -1,5 +1,13 @@
 """Learned frontier ordering: traces -> training -> held-out evaluation.
 
+The committed scorer (sgfim/data/scorer_weights.npz) was trained by the
+project's own kernels on traces of 200 seeded 20,000-transaction streams at a
+6% floor:
+
+    python -m sgfim.learned_order --train-seeds 200 --n-txn 20000 --floor 0.06 \
+        --eval-seeds 20 --eval-n-txn 2000000 --eval-floor 0.03 \
+        --save-weights sgfim/data/scorer_weights.npz --out learned.json
+
 Workload family: the anytime-2m generator (80 sensors x 8 bins = 640 items,
 one item per sensor per transaction, 32 latent regimes, Dirichlet(0.2) bin
 probabilities), with a per-stream seed.  The plain miner (siblings visited by
@@ -46,7 +54,10 @@ def collect_traces(eng, seeds, n_txn, floor, order="support_desc"):
 
 
 def coverage_times(res):
-    return {f"t{int(f * 100)}": res.time_to_coverage(f) for f in COVERAGE}
+    """Seconds and search nodes until 50/90/95% of the final MFIs were emitted."""
+    out = {f"t{int(f * 100)}": res.time_to_coverage(f) for f in COVERAGE}
+    out.update({f"n{int(f * 100)}": res.nodes_to_coverage(f) for f in COVERAGE})
+    return out
 
 
 def evaluate(eng, seeds, n_txn, floor, reps=1):
@@ -71,12 +82,34 @@ def evaluate(eng, seeds, n_txn, floor, reps=1):
 
 
 def summarize(rows):
-    out = {"identical_all": all(r["identical"] for r in rows)}
-    for key in ("t50", "t90", "t95", "total_s"):
-        ratio = [r["learned"][key] / max(r["support_desc"][key], 1e-9) for r in rows]
-        out[f"{key}_ratio_median"] = float(np.median(ratio))
-        out[f"{key}_ratio_geomean"] = float(np.exp(np.mean(np.log(np.maximum(ratio, 1e-9)))))
+    """Learned / support-descending ratios (geomean and median over seeds) of the
+    time and of the search nodes to each coverage level, and the same for the
+    canonical order (lowest-support sibling first)."""
+    out = {"identical_all": all(r["identical"] for r in rows), "seeds": len(rows),
+           "nodes_equal_all_orders": all(r["learned"]["nodes"] == r["support_desc"]["nodes"] == r["support"]["nodes"]
+                                         for r in rows)}
+    for order in ("learned", "support"):
+        for key in ("t50", "t90", "t95", "n50", "n90", "n95", "total_s"):
+            ratio = [r[order][key] / max(r["support_desc"][key], 1e-9) for r in rows]
+            pre = "" if order == "learned" else "canonical_"
+            out[f"{pre}{key}_ratio_median"] = float(np.median(ratio))
+            out[f"{pre}{key}_ratio_geomean"] = float(np.exp(np.mean(np.log(np.maximum(ratio, 1e-9)))))
     return out
+
+
+def load_weights(eng, path):
+    w = np.load(path)
+    eng.load_scorer(w["W1"], w["b1"], w["W2"], w["b2"], w["w3"], w["b3"])
+
+
+def evaluate_committed(weights_path, n_seeds=3, n_txn=2_000_000, floor=0.03, first_seed=5010):
+    """Held-out streams of the anytime-2m family with committed scorer weights:
+    coverage times and nodes of the learned, canonical and support-descending
+    orders, final sets compared."""
+    with Engine() as eng:
+        load_weights(eng, weights_path)
+        rows = evaluate(eng, range(first_seed, first_seed + n_seeds), n_txn, floor)
+    return {"n_txn": n_txn, "floor": floor, "summary": summarize(rows), "runs": rows}
 
 
 def main(argv=None):
@@ -86,6 +119,8 @@ def main(argv=None):
     ap.add_argument("--n-txn", type=int, default=20000)
     ap.add_argument("--floor", type=float, default=0.06)
     ap.add_argument("--eval-n-txn", type=int, default=0)
+    ap.add_argument("--eval-floor", type=float, default=0.0)
+    ap.add_argument("--save-weights", default="", help="write the trained scorer (.npz)")
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
@@ -102,13 +137,16 @@ def main(argv=None):
     acc = float(((P > 0.5) == (Y > 0.5)).mean())
     w = tr.weights()
     eng.load_scorer(w["W1"], w["b1"], w["W2"], w["b2"], w["w3"], w["b3"])
+    if a.save_weights:
+        np.savez(a.save_weights, **w)
     ev_n = a.eval_n_txn or a.n_txn
-    rows = evaluate(eng, range(5000, 5000 + a.eval_seeds), ev_n, a.floor)
+    ev_floor = a.eval_floor or a.floor
+    rows = evaluate(eng, range(5000, 5000 + a.eval_seeds), ev_n, ev_floor)
     summ = summarize(rows)
     report = {"train": {"seeds": a.train_seeds, "n_txn": a.n_txn, "floor": a.floor, "rows": int(len(Y)),
                         "positive_rate": float(Y.mean()), "trace_s": t_trace, "train_s": t_train,
                         "loss": hist, "train_accuracy": acc},
-              "eval": {"seeds": a.eval_seeds, "n_txn": ev_n, "floor": a.floor, "summary": summ, "runs": rows}}
+              "eval": {"seeds": a.eval_seeds, "n_txn": ev_n, "floor": ev_floor, "summary": summ, "runs": rows}}
     print(json.dumps({"train": report["train"], "summary": summ}))
     if a.out:
         with open(a.out, "w") as f:

@@ -275,6 +275,8 @@ typedef struct {
      * the next phase): [0] extension counts, [1] pool (HUT / leaf) queries,
      * [2] FHUT counts, [3] final maximality filter, [4] scoring, [5] the rest */
     double phase_s[6];
+    uint64_t *emit_node;     /* search nodes expanded when each set was emitted (a clock-free
+                                measure of how early the search order reaches it) */
 } sgfim_result;
 
 #define SGFIM_TRACE_DIM 8
@@ -286,7 +288,8 @@ typedef struct {
 
 /* Frontier orders: the order in which sibling subtrees are searched.  The
  * tree itself (every node's tail: the frequent extensions of higher support)
- * and the final result never change; only the emission order does. */
+ * and the final result never change; only the emission order does (node counts
+ * are the same in every order, at every wave size). */
 #define SGFIM_ORDER_SUPPORT 0      /* canonical: lowest-support sibling first */
 #define SGFIM_ORDER_LEARNED 1      /* highest score of the loaded scoring MLP first */
 #define SGFIM_ORDER_SUPPORT_DESC 2 /* highest-support sibling first (the reference's frequency order) */

@@ -491,15 +491,16 @@ int sgfim_cooccurrence_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t
                               uint64_t row_stride, uint32_t *out, int kind, void *stream) {
     if (!h || (d && (!bitmaps || !out))) return fail(h, SGFIM_EINVAL, "null argument");
     if (row_stride & 1) return fail(h, SGFIM_EINVAL, "row_stride must be even");
-    if (kind < 0 || kind > 3) return fail(h, SGFIM_EINVAL, "unknown co-occurrence kernel");
+    if (kind < 0 || kind > 4) return fail(h, SGFIM_EINVAL, "unknown co-occurrence kernel");
     API_GUARD_BEGIN
     cudaSetDevice(h->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (cudaStream_t)0;
-    // AUTO: the tcgen05 e4m3 GEMM (the fastest on GB300, 1.33 ms vs 4.97 ms for the CUDA-core
-    // popcount at 1,024 x 1,024 x 2^20); the popcount kernel when the layout does not suit it
+    // AUTO: the tcgen05 e4m3 GEMM with 256 x 256 blocks (the fastest on GB300 at
+    // 1,024 x 1,024 x 2^20: 0.53 ms, against 1.29 ms with 128 x 128 tiles and 4.97 ms for the
+    // CUDA-core popcount); the popcount kernel when the layout does not suit it
     int rc = -1;
     if (kind == SGFIM_COOC_AUTO) {
-        rc = cooc_device(bitmaps, d, n_words, row_stride, out, SGFIM_COOC_TC_F8, st, h->n_sm, nullptr, 0,
+        rc = cooc_device(bitmaps, d, n_words, row_stride, out, SGFIM_COOC_TC_F8_256, st, h->n_sm, nullptr, 0,
                          &h->launches, h->dev_err.as<uint32_t>());
         if (rc == 0) return SGFIM_OK;
         kind = SGFIM_COOC_POPC;

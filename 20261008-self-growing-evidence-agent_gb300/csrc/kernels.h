@@ -127,6 +127,9 @@ int cooc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t 
                 int kind, cudaStream_t st, int n_sm, void *scratch, size_t scratch_bytes, uint64_t *launches,
                 uint32_t *dev_err = nullptr);
 // tcgen05 e4m3 GEMM form (kernels_tc.cu); returns -1 when the layout is unusable.
+// 256 x 256 blocks (two M = 128, N = 256 MMAs per K step), the AUTO form.
+int cooc_tc256_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
+                      cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches);
 int cooc_tc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,
                    cudaStream_t st, int n_sm, uint32_t *dev_err, uint64_t *launches);
 size_t cooc_scratch_bytes(uint32_t d, uint64_t n_words, int kind);

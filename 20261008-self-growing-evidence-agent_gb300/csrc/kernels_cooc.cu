@@ -190,6 +190,7 @@ int cooc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t 
     (void)scratch; (void)scratch_bytes;
     if (d == 0) return 0;
     if (kind == 3) return cooc_tc_device(bitmaps, d, n_words, row_stride, out, st, n_sm, dev_err, launches);
+    if (kind == 4) return cooc_tc256_device(bitmaps, d, n_words, row_stride, out, st, n_sm, dev_err, launches);
     SG_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)d * d * 4, st));
     const uint32_t n_tiles = (d + kPT - 1) / kPT;
     const uint32_t pairs = n_tiles * (n_tiles + 1) / 2;

@@ -24,7 +24,7 @@ NOALLOC_MAX_CAND = 1048576
 ROOTS_ALL, ROOTS_LIST, ROOTS_MINCOUNT = 0, 1, 2
 ORDER_SUPPORT, ORDER_LEARNED, ORDER_SUPPORT_DESC = 0, 1, 2
 TRACE_DIM = 8
-COOC_AUTO, COOC_POPC, COOC_BMMA, COOC_TC_F8 = 0, 1, 2, 3
+COOC_AUTO, COOC_POPC, COOC_BMMA, COOC_TC_F8, COOC_TC_F8_256 = 0, 1, 2, 3, 4
 
 
 class Config(C.Structure):

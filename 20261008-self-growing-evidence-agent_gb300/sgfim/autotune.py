@@ -19,7 +19,7 @@ SUPPORT_PLANS = [("lane", 0, 0), ("lane", 0, 3), ("lane", 0, 4),
                  ("staged", 0, 0), ("staged", 0, 1), ("staged", 0, 3), ("staged4", 0, 0), ("staged4", 0, 1),
                  ("sorted", 0, 0), ("sorted", 0, 2),
                  ("stream", 0, 0)]
-COOC_KINDS = [(1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3")]
+COOC_KINDS = [(1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3"), (4, "tcgen05_e4m3_256")]
 
 
 def _bucket(x):

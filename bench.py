@@ -567,8 +567,8 @@ def main():
     # the 1,024 x 1,024 co-occurrence matrix of the same bitmaps (every kernel kind)
     cooc = {}
     if not args.no_cooc and world == 1:
-        t_co = {k: torch.zeros(d * d, dtype=torch.int32, device=dev) for k in (1, 2, 3)}
-        for kind, name in ((1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3")):
+        t_co = {k: torch.zeros(d * d, dtype=torch.int32, device=dev) for k in (1, 2, 3, 4)}
+        for kind, name in ((1, "popc"), (2, "bmma_b1"), (3, "tcgen05_e4m3"), (4, "tcgen05_e4m3_256")):
             for _ in range(2):
                 eng.cooccurrence_device(t_bm.data_ptr(), d, n_words, n_words, t_co[kind].data_ptr(), kind,
                                         stream.cuda_stream)
@@ -586,7 +586,7 @@ def main():
             ms_c = statistics.median(times)
             bitops = float(d) * d * WORKLOAD["n_txn"]
             cooc[name] = {"ms": ms_c, "tbitops": bitops / (ms_c / 1000.0) / 1e12}
-        cooc["kinds_agree"] = bool(torch.equal(t_co[1], t_co[2]) and torch.equal(t_co[1], t_co[3]))
+        cooc["kinds_agree"] = bool(all(torch.equal(t_co[1], t_co[k]) for k in (2, 3, 4)))
 
     cpu = cpu_np = None
     gpu_sup = t_out.cpu().numpy().view(np.uint32)

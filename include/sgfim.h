@@ -224,12 +224,13 @@ typedef struct {
 int sgfim_phase_stats_get(sgfim_handle *h, sgfim_phase_stats *out, int reset);
 
 /* Device-pointer form: bitmaps as in sgfim_support_batch_device, out d*d
- * uint32 in device memory.  kind: SGFIM_COOC_* (AUTO: the tcgen05 kernel, or the popcount
- * kernel when the bitmaps are not 16-byte aligned). */
+ * uint32 in device memory.  kind: SGFIM_COOC_* (AUTO: the tcgen05 kernel with 256 x 256
+ * blocks, or the popcount kernel when the bitmaps are not 16-byte aligned). */
 #define SGFIM_COOC_AUTO 0
 #define SGFIM_COOC_POPC 1     /* CUDA-core AND + popc, register tiled */
 #define SGFIM_COOC_BMMA 2     /* b1 mma.sync AND-POPC on the tensor pipe */
-#define SGFIM_COOC_TC_F8 3    /* tcgen05 e4m3 GEMM of 0/1 bytes, fp32 accumulate */
+#define SGFIM_COOC_TC_F8 3    /* tcgen05 e4m3 GEMM of 0/1 bytes, fp32 accumulate, 128 x 128 tiles */
+#define SGFIM_COOC_TC_F8_256 4 /* the same with 256 x 256 blocks (two M=128, N=256 MMAs per K step) */
 int sgfim_cooccurrence_device(sgfim_handle *h, const uint64_t *bitmaps, uint32_t d, uint64_t n_words,
                               uint64_t row_stride, uint32_t *out, int kind, void *stream);
 

@@ -138,8 +138,8 @@ def test_support_full_size_sample(engine):
     assert (parent >= got).all()
 
 
-@pytest.mark.parametrize("kind", [1, 2, 3])
-@pytest.mark.parametrize("n_txn,d", [(4096, 24), (65536 + 64, 300), (1 << 16, 256), (100_032, 130)])
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
+@pytest.mark.parametrize("n_txn,d", [(4096, 24), (65536 + 64, 300), (1 << 16, 256), (100_032, 130), (200_064, 700)])
 def test_cooccurrence_matches_oracle(engine, kind, n_txn, d):
     torch = pytest.importorskip("torch")
     bm = _bitmaps(n_txn, d, seed=d + kind)

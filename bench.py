@@ -612,6 +612,10 @@ def main():
             configs["anytime_2m"] = {k: aw[k] for k in ("floor", "min_count", "mfis", "nodes", "mine_s", "time_to",
                                                          "gen_s", "load_s")}
             configs["anytime_2m"]["coverage"] = {str(c["t_s"]): c["coverage"] for c in aw["checkpoints"]}
+        lw = configs.get("learned_order", {})
+        if "summary" in lw:
+            configs["learned_order"] = {"n_txn": lw["n_txn"], "floor": lw["floor"], "summary": lw["summary"],
+                                        "seeds": [r["seed"] for r in lw["runs"]]}
         ww = configs.get("windows_4096", {})
         if "p50_ms" in ww:
             configs["windows_4096"] = {k: ww[k] for k in ("requests", "rate_hz", "windows", "errors", "p50_ms",

@@ -31,7 +31,7 @@ def test_autotune_support_and_cooc(engine, tmp_path):
         assert np.array_equal(out.cpu().numpy().view(np.uint32), oracle.support_batch(bm, cp, ci))
         co = torch.zeros(d * d, dtype=torch.int32, device=dev)
         kind, cms = tuner.tune_cooc(tb, d, w, w, co)
-        assert kind in cms and len(cms) == 3
+        assert kind in cms and len(cms) == 4
         assert np.array_equal(co.cpu().numpy().view(np.uint32).reshape(d, d), oracle.cooccurrence(bm))
         saved = json.load(open(cache))
         assert len(saved) == 2

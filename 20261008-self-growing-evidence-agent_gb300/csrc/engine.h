@@ -138,14 +138,16 @@ struct WindowWorkspace {
 // that repeated mining (anytime stages, window services) allocates nothing
 // once warm.
 struct MinerWorkspace {
-    DevBuf arena, pool, q_out, score, cooc, t_out;
+    DevBuf arena, pool, q_out, score, cooc, t_out, pdb, pofs;
     HostBuf hq_out, hscore, ht_out;
-    Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat, w0, t_ptr, t_items, t_slot;
+    Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat, w0, t_ptr, t_items, t_slot,
+        p_items_list;
     void release() {
         arena.release(); pool.release(); q_out.release(); score.release(); cooc.release(); t_out.release();
+        pdb.release(); pofs.release();
         hq_out.release(); hscore.release(); ht_out.release();
         for (Staged *s : {&q_ptr, &q_items, &q_slot, &c_ptr, &c_items, &c_ps, &c_cs, &p_ptr, &p_items, &feat, &w0,
-                          &t_ptr, &t_items, &t_slot})
+                          &t_ptr, &t_items, &t_slot, &p_items_list})
             s->release();
     }
 };

@@ -946,6 +946,75 @@ void launch_wait_probe(uint32_t *err, cudaStream_t st) {
     SG_CUDA_TRY(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------- projected databases
+// Exclusive prefix popcounts of a row's words (one CTA): ofs[w] = set bits of
+// words 0 .. w-1, the position of word w's first transaction in the projection.
+__global__ void __launch_bounds__(1024) row_prefix_kernel(const uint64_t *__restrict__ row, uint64_t n_words,
+                                                          uint32_t *__restrict__ ofs) {
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x;
+    const uint64_t per = (n_words + 1023) / 1024;
+    const uint64_t w0 = min(n_words, (uint64_t)t * per), w1 = min(n_words, w0 + per);
+    uint32_t s = 0;
+    for (uint64_t w = w0; w < w1; ++w) s += popc64(row[w]);
+    part[t] = s;
+    __syncthreads();
+    for (uint32_t o = 1; o < 1024; o <<= 1) {   // inclusive scan
+        const uint32_t v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;
+    for (uint64_t w = w0; w < w1; ++w) {
+        ofs[w] = run;
+        run += popc64(row[w]);
+    }
+}
+
+// Row items[blockIdx.y] of the projection: the bits of that bitmap row at the set
+// positions of `root`, packed in transaction order (out rows zeroed beforehand).
+__global__ void project_rows_kernel(const uint64_t *__restrict__ rows, uint64_t stride, uint64_t n_words,
+                                    const uint64_t *__restrict__ root, const uint32_t *__restrict__ ofs,
+                                    const uint32_t *__restrict__ items, unsigned long long *__restrict__ out,
+                                    uint64_t out_stride) {
+    const uint32_t e = items[blockIdx.y];
+    const uint64_t *src = rows + (uint64_t)e * stride;
+    unsigned long long *dst = out + (uint64_t)e * out_stride;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t m = root[w];
+        if (!m) continue;
+        const uint64_t v = src[w];
+        uint64_t p = 0;
+        uint32_t nb = 0;
+        while (m) {   // bit extraction under the mask, lowest transaction first
+            const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
+            p |= ((v >> b) & 1ull) << nb;
+            ++nb;
+            m &= m - 1;
+        }
+        if (!p) continue;
+        const uint32_t o = ofs[w], sh = o & 63;
+        atomicOr(dst + (o >> 6), (unsigned long long)(p << sh));
+        if (sh && sh + nb > 64) atomicOr(dst + (o >> 6) + 1, (unsigned long long)(p >> (64 - sh)));
+    }
+}
+
+void launch_projection(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t root_row,
+                       const uint32_t *items, uint32_t n_items, uint32_t *ofs, uint64_t *out, uint64_t out_stride,
+                       uint64_t out_words, uint32_t d, cudaStream_t st, int n_sm) {
+    SG_CUDA_TRY(cudaMemset2DAsync(out, out_stride * 8, 0, out_words * 8, d, st));
+    if (n_items == 0 || n_words == 0) return;
+    const uint64_t *root = rows + (uint64_t)root_row * stride;
+    row_prefix_kernel<<<1, 1024, 0, st>>>(root, n_words, ofs);
+    SG_CUDA_TRY(cudaGetLastError());
+    const unsigned bx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_words + 255) / 256,
+                                                                            (uint64_t)n_sm * 16 / std::max(1u, n_items) + 1));
+    project_rows_kernel<<<dim3(bx, n_items), 256, 0, st>>>(rows, stride, n_words, root, ofs, items,
+                                                           reinterpret_cast<unsigned long long *>(out), out_stride);
+    SG_CUDA_TRY(cudaGetLastError());
+}
+
 // ---------------------------------------------------------------- miner helpers
 __global__ void child_mask_kernel(uint64_t *__restrict__ arena, uint64_t astride, uint64_t n_words,
                                   const uint64_t *__restrict__ rows, uint64_t rstride, const uint64_t *__restrict__ ptr,

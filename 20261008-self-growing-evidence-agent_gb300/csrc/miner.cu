@@ -22,6 +22,16 @@
 // the final maximality filter counts, for every candidate, the pool members
 // that contain it; exactly one (itself) means the candidate is maximal.
 //
+// Projection: on large datasets every root subtree (the root child H = {r}
+// and all its descendants) is searched on r's projected database -- each
+// row restricted to the transactions holding r, packed -- so tidset masks,
+// tail counts, FHUT counts and child masks are sup(r)/N as long as on the
+// whole database.  Up to kProjSlots projections are resident in one buffer
+// (slot p's row e is row p*d + e of it), a projection is built on the device
+// when its root child is popped, and its slot is reused once no node of the
+// subtree is left; a wave may hold nodes of several resident projections, and
+// its queries address rows through the slot of each node's projection.
+//
 // The order in which sibling subtrees are searched is a policy (canonical
 // ascending support, support descending, or the learned scorer); the tree,
 // every count and the final set do not depend on it.
@@ -46,6 +56,8 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr uint32_t kNoNode = 0xffffffffu;
+constexpr uint32_t kNoProj = 0xffffffffu;
+constexpr uint32_t kProjSlots = 8;
 constexpr uint32_t kDim = SGFIM_TRACE_DIM;
 
 struct MNode {
@@ -54,6 +66,7 @@ struct MNode {
     uint32_t sup = 0;
     uint32_t slot = kNoSlot;     // tidset mask slot; kNoSlot = AND of head rows
     uint32_t id = 0;             // search-tree node id
+    uint32_t proj = kNoProj;     // root item whose projected database the node's masks live in
 };
 
 struct QuerySet {
@@ -106,6 +119,40 @@ class Miner {
     DevBuf &arena_;
     uint64_t slot_words_ = 0;
     std::vector<uint32_t> free_slots_;
+    // the bitmap view the wave's queries read: the whole database, or the
+    // buffer of resident projections (rows translated per node by prow)
+    const uint64_t *vrows_ = nullptr;
+    uint64_t vstride_ = 0, vwords_ = 0;
+    uint32_t vd_ = 0;                    // rows of the view (queries read item indices below it)
+    bool use_proj_ = false;
+    uint64_t proj_stride_ = 0;
+    uint32_t n_proj_slots_ = 0;
+    uint64_t projections_ = 0;
+    std::vector<uint32_t> slot_root_;    // projection slot -> root item (kNoProj: free)
+    std::vector<int32_t> root_slot_;     // root item -> slot (-1: not resident)
+    std::vector<uint32_t> live_;         // root item -> nodes of its subtree on the stack or in the wave
+    std::vector<uint64_t> wp_;           // root item -> words of its projection
+    void view_global() {
+        vrows_ = ds_.bitmaps.as<uint64_t>();
+        vstride_ = ds_.stride;
+        vwords_ = ds_.n_words;
+        vd_ = ds_.d;
+    }
+    bool make_resident(const MNode &nd);
+    // row of item e for queries of node nd under the current view
+    uint32_t prow(const MNode &nd, uint32_t e) const {
+        return (use_proj_ && nd.proj != kNoProj) ? (uint32_t)root_slot_[nd.proj] * ds_.d + e : e;
+    }
+    void add_query(QuerySet &q, const MNode &nd, const uint32_t *it, size_t k, uint32_t slot) {
+        if (!use_proj_ || nd.proj == kNoProj) {
+            q.add(it, k, slot);
+            return;
+        }
+        const uint32_t off = (uint32_t)root_slot_[nd.proj] * ds_.d;
+        for (size_t i = 0; i < k; ++i) q.items.push_back(it[i] + off);
+        q.ptr.push_back(q.items.size());
+        q.slot.push_back(slot);
+    }
     // device pool (rows = items, one bit per candidate), in the workspace
     DevBuf &pool_;
     uint64_t pool_words_ = 0;
@@ -204,7 +251,7 @@ void Miner::run_tail_counts(const std::vector<uint64_t> &ptr, const std::vector<
     const uint32_t *dslot = w_.t_slot.put(slots.data(), slots.size(), st);
     w_.t_out.reserve(n * 4, st);
     w_.ht_out.reserve(n * 4);
-    launch_tail_counts(ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, arena_.as<uint64_t>(), slot_words_, dslot,
+    launch_tail_counts(vrows_, vstride_, vwords_, arena_.as<uint64_t>(), slot_words_, dslot,
                        dptr, (uint32_t)slots.size(), n, ditems, w_.t_out.as<uint32_t>(), st, h_->n_sm);
     ++launches_;
     SG_CUDA_TRY(cudaMemcpyAsync(w_.ht_out.ptr, w_.t_out.ptr, n * 4, cudaMemcpyDeviceToHost, st));
@@ -327,6 +374,34 @@ void Miner::score(const std::vector<float> &feat, size_t n, std::vector<float> &
     memcpy(out.data(), hscore_.ptr, n * 4);
 }
 
+// Make `nd`'s root subtree resident: build its projected database (the rows of
+// its head and tail items; the root item's own row becomes all ones) in a free
+// slot, or in the slot of a subtree with no node left.  False when every slot
+// holds a live subtree.
+bool Miner::make_resident(const MNode &nd) {
+    int32_t slot = -1;
+    for (uint32_t p = 0; p < n_proj_slots_ && slot < 0; ++p)
+        if (slot_root_[p] == kNoProj || live_[slot_root_[p]] == 0) slot = (int32_t)p;
+    if (slot < 0) return false;
+    if (slot_root_[slot] != kNoProj) root_slot_[slot_root_[slot]] = -1;
+    cudaStream_t st = h_->stream;
+    const uint32_t r = nd.proj;
+    std::vector<uint32_t> items(nd.head.begin(), nd.head.end());
+    items.insert(items.end(), nd.tail.begin(), nd.tail.end());
+    const uint32_t *ditems = w_.p_items_list.put(items.data(), items.size(), st);
+    // whole rows are cleared: a wave reads up to its widest projection, so every
+    // row must be zero past its own projection's words
+    launch_projection(ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, r, ditems, (uint32_t)items.size(),
+                      w_.pofs.as<uint32_t>(), w_.pdb.as<uint64_t>() + (uint64_t)slot * ds_.d * proj_stride_,
+                      proj_stride_, proj_stride_, ds_.d, st, h_->n_sm);
+    launches_ += 2;
+    ++projections_;
+    slot_root_[slot] = r;
+    root_slot_[r] = slot;
+    wp_[r] = ((ds_.sup[r] + 63) / 64 + 1) & ~1ull;
+    return true;
+}
+
 int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *user, sgfim_result **out) {
     *out = nullptr;
     if (!ds_.loaded) return fail(h_, SGFIM_ESTATE, "no dataset loaded");
@@ -350,8 +425,26 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         if (ds_.sup[e] >= thr_) freq.push_back(e);
     std::stable_sort(freq.begin(), freq.end(), [&](uint32_t a, uint32_t b) { return ds_.sup[a] < ds_.sup[b]; });
 
+    // projected root subtrees on large datasets (SGFIM_F_NO_PROJECTION / SGFIM_F_PROJECT override)
+    view_global();
+    use_proj_ = (h_->flags & SGFIM_F_PROJECT) ||
+                (!(h_->flags & SGFIM_F_NO_PROJECTION) && ds_.n_words >= 2048 && freq.size() > 1);
+    if (use_proj_) {
+        uint64_t wmax = 2;
+        for (uint32_t e : freq) wmax = std::max<uint64_t>(wmax, ((ds_.sup[e] + 63) / 64 + 1) & ~1ull);
+        proj_stride_ = wmax;
+        const uint64_t slot_bytes = (uint64_t)d * wmax * 8;
+        n_proj_slots_ = (uint32_t)std::max<uint64_t>(
+            1, std::min<uint64_t>(kProjSlots, (h_->hbm_budget / 8) / std::max<uint64_t>(slot_bytes, 1)));
+        w_.pdb.reserve((size_t)n_proj_slots_ * slot_bytes, st);
+        w_.pofs.reserve((size_t)std::max<uint64_t>(ds_.n_words, 1) * 4, st);
+        slot_root_.assign(n_proj_slots_, kNoProj);
+        root_slot_.assign(d, -1);
+        live_.assign(d, 0);
+        wp_.assign(d, 0);
+    }
     // mask arena
-    slot_words_ = ds_.stride;
+    slot_words_ = use_proj_ ? proj_stride_ : ds_.stride;
     const uint64_t slot_bytes = slot_words_ * 8;
     const uint64_t budget = h_->hbm_budget / 4;
     uint64_t max_slots = std::min<uint64_t>(1u << 20, budget / std::max<uint64_t>(slot_bytes, 1));
@@ -406,12 +499,34 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         wave.clear();
         uint64_t nq = 0;
+        bool wave_global = !use_proj_;
+        uint64_t wave_words = 0;
         while (!stack.empty() && wave.size() < nmax) {
+            if (use_proj_) {
+                const MNode &top = stack.back();
+                if (top.proj == kNoProj) {   // the root node: the whole database
+                    if (!wave.empty() && !wave_global) break;
+                    wave_global = true;
+                } else {
+                    if (wave_global && !wave.empty()) break;
+                    wave_global = false;
+                    if (root_slot_[top.proj] < 0 && !make_resident(top)) break;
+                    wave_words = std::max(wave_words, wp_[top.proj]);
+                }
+            }
             const uint64_t w = stack.back().tail.size();
             if (!wave.empty() && nq + w > qmax) break;
             nq += w;
             wave.push_back(std::move(stack.back()));
             stack.pop_back();
+        }
+        if (wave_global) {
+            view_global();
+        } else {
+            vrows_ = w_.pdb.as<uint64_t>();
+            vstride_ = proj_stride_;
+            vwords_ = wave_words;
+            vd_ = n_proj_slots_ * d;   // slot p's row e is row p * d + e
         }
         ++waves_;
         nodes_ += wave.size();
@@ -423,14 +538,14 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             if (nd.slot != kNoSlot || nd.head.empty() || nd.tail.size() < 2) continue;
             const uint32_t s = alloc_slot();
             if (s == kNoSlot) break;
-            qchild.add(nd.head.data(), nd.head.size(), kNoSlot);
+            add_query(qchild, nd, nd.head.data(), nd.head.size(), kNoSlot);
             child_slot.push_back(s);
             nd.slot = s;
         }
         if (qchild.size()) {
             const size_t n = qchild.size();
-            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(),
-                               ds_.stride, c_ptr_.put(qchild.ptr.data(), n + 1, st),
+            launch_child_masks(arena_.as<uint64_t>(), slot_words_, vwords_, vrows_, vstride_,
+                               c_ptr_.put(qchild.ptr.data(), n + 1, st),
                                c_items_.put(qchild.items.data(), qchild.items.size(), st),
                                c_ps_.put(qchild.slot.data(), n, st), c_cs_.put(child_slot.data(), n, st), (uint32_t)n,
                                st, h_->n_sm);
@@ -448,7 +563,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             if (nd.slot != kNoSlot) {
                 count_src[i] = {0, t_items.size()};
                 if (nd.tail.empty()) continue;
-                t_items.insert(t_items.end(), nd.tail.begin(), nd.tail.end());
+                for (uint32_t e : nd.tail) t_items.push_back(prow(nd, e));
                 t_ptr.push_back(t_items.size());
                 t_slot.push_back(nd.slot);
             } else {
@@ -456,13 +571,13 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 for (uint32_t e : nd.tail) {
                     tmp.assign(nd.head.begin(), nd.head.end());
                     tmp.push_back(e);
-                    qs.add(tmp.data(), tmp.size(), kNoSlot);
+                    add_query(qs, nd, tmp.data(), tmp.size(), kNoSlot);
                 }
             }
         }
         timed(0, [&] {
             run_tail_counts(t_ptr, t_items, t_slot, counts);
-            run_queries(qs, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, counts_q);
+            run_queries(qs, vrows_, vstride_, vwords_, vd_, QUERY_COUNT, counts_q);
         });
         // ---- phase B: PEP, ordering, pool and FHUT queries
         // Work records keep their vectors' capacity from wave to wave
@@ -495,8 +610,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 // tmp = head, then F: the FHUT query of a masked node takes the F part
                 wk.kind = 1;
                 wk.fhut_q = qfhut.size();
-                if (nd.slot != kNoSlot) qfhut.add(tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
-                else qfhut.add(tmp.data(), tmp.size(), kNoSlot);
+                if (nd.slot != kNoSlot) add_query(qfhut, nd, tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
+                else add_query(qfhut, nd, tmp.data(), tmp.size(), kNoSlot);
             }
             // the pool query lists the rarest pool rows first: the device AND empties
             // sooner and stops reading rows
@@ -511,7 +626,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         } else {
             pool_hit.assign(qpool.size(), 0);
         }
-        timed(2, [&] { run_queries(qfhut, ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, d, QUERY_COUNT, fhut_cnt); });
+        timed(2, [&] { run_queries(qfhut, vrows_, vstride_, vwords_, vd_, QUERY_COUNT, fhut_cnt); });
         // ---- phase C: emit candidates, create children
         const uint64_t pool_before = csup_.size();
         kids.clear();
@@ -544,6 +659,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 c.tail.reserve(nf - j - 1);
                 for (size_t k = j + 1; k < nf; ++k) c.tail.push_back(wk.f[k].second);
                 c.id = (uint32_t)parent_.size();
+                c.proj = (use_proj_ && nd.proj == kNoProj) ? wk.f[j].second : nd.proj;
                 parent_.push_back(nd.id);
                 if (need_feat_) {
                     float f[kDim];
@@ -565,11 +681,16 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         child_slot.clear();
         for (size_t k = 0; k < kids.size(); ++k) {
             MNode &c = kids[k];
-            if (c.tail.empty()) continue;  // leaves need no mask
+            // leaves need no mask; a root child gets its mask once its projection is resident
+            if (c.tail.empty() || (use_proj_ && (c.proj == kNoProj || root_slot_[c.proj] < 0))) continue;
             c.slot = alloc_slot();
             if (c.slot == kNoSlot) continue;
-            if (kid_src[k].first != kNoSlot) qchild.add(&kid_src[k].second, 1, kid_src[k].first);
-            else qchild.add(c.head.data(), c.head.size(), kNoSlot);
+            if (kid_src[k].first != kNoSlot) {
+                const uint32_t e = prow(c, kid_src[k].second);
+                qchild.add(&e, 1, kid_src[k].first);
+            } else {
+                add_query(qchild, c, c.head.data(), c.head.size(), kNoSlot);
+            }
             child_slot.push_back(c.slot);
         }
         if (qchild.size()) {
@@ -578,8 +699,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             const uint32_t *ditems = c_items_.put(qchild.items.data(), qchild.items.size(), st);
             const uint32_t *dps = c_ps_.put(qchild.slot.data(), n, st);
             const uint32_t *dcs = c_cs_.put(child_slot.data(), n, st);
-            launch_child_masks(arena_.as<uint64_t>(), slot_words_, ds_.n_words, ds_.bitmaps.as<uint64_t>(),
-                               ds_.stride, dptr, ditems, dps, dcs, (uint32_t)n, st, h_->n_sm);
+            launch_child_masks(arena_.as<uint64_t>(), slot_words_, vwords_, vrows_, vstride_, dptr, ditems, dps,
+                               dcs, (uint32_t)n, st, h_->n_sm);
             ++launches_;
         }
         // sibling visiting order
@@ -594,11 +715,16 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             } else if (p_.order == SGFIM_ORDER_LEARNED) {
                 std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return wscore[a] > wscore[b]; });
             }
-            for (size_t j = ord.size(); j-- > 0;) stack.push_back(std::move(kids[ord[j]]));
+            for (size_t j = ord.size(); j-- > 0;) {
+                if (use_proj_ && kids[ord[j]].proj != kNoProj) ++live_[kids[ord[j]].proj];
+                stack.push_back(std::move(kids[ord[j]]));
+            }
         }
         // parents' masks are no longer needed once the child-mask kernel ran (stream order)
-        for (MNode &nd : wave)
+        for (MNode &nd : wave) {
             if (nd.slot != kNoSlot) free_slots_.push_back(nd.slot);
+            if (use_proj_ && nd.proj != kNoProj) --live_[nd.proj];
+        }
         flush_pool(pool_before);
         // ---- checkpoints, limits
         const double el = elapsed();

@@ -69,6 +69,7 @@ class PhaseStats(C.Structure):
 
 F_VERBOSE, F_IGNORE_ID0, F_PHASE_TIMERS, F_BLOCKING_SYNC = 0x1, 0x2, 0x4, 0x8
 F_WINDOWS_HORIZONTAL = 0x10
+F_NO_PROJECTION, F_PROJECT = 0x20, 0x40
 TX_LOAD = 0x1
 TX_P2_FULL = 0x2
 

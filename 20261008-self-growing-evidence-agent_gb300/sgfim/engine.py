@@ -90,11 +90,14 @@ class MineResult:
 
 class Engine:
     def __init__(self, device=0, hbm_budget=0, wave_nodes=0, verbose=False, phase_timers=False,
-                 ignore_id0=False, blocking_sync=False, windows_horizontal=False, wait_limit_us=0):
+                 ignore_id0=False, blocking_sync=False, windows_horizontal=False, wait_limit_us=0, projection=None):
+        """projection: None = the miner decides by size, True = always project root
+        subtrees, False = never (see SGFIM_F_PROJECT / SGFIM_F_NO_PROJECTION)."""
         self._L = L.load()
         flags = (L.F_VERBOSE if verbose else 0) | (L.F_PHASE_TIMERS if phase_timers else 0) | \
             (L.F_IGNORE_ID0 if ignore_id0 else 0) | (L.F_BLOCKING_SYNC if blocking_sync else 0) | \
-            (L.F_WINDOWS_HORIZONTAL if windows_horizontal else 0)
+            (L.F_WINDOWS_HORIZONTAL if windows_horizontal else 0) | \
+            (L.F_PROJECT if projection is True else L.F_NO_PROJECTION if projection is False else 0)
         cfg = L.Config(device, hbm_budget, wave_nodes, flags, None, wait_limit_us)
         h = C.c_void_p()
         rc = self._L.sgfim_open(C.byref(cfg), C.byref(h))

@@ -89,7 +89,7 @@ def summarize(rows):
            "nodes_equal_all_orders": all(r["learned"]["nodes"] == r["support_desc"]["nodes"] == r["support"]["nodes"]
                                          for r in rows)}
     for order in ("learned", "support"):
-        for key in ("t50", "t90", "t95", "n50", "n90", "n95", "total_s"):
+        for key in ("t50", "t90", "t95", "n50", "n90", "n95", "total_s", "nodes"):
             ratio = [r[order][key] / max(r["support_desc"][key], 1e-9) for r in rows]
             pre = "" if order == "learned" else "canonical_"
             out[f"{pre}{key}_ratio_median"] = float(np.median(ratio))

@@ -73,6 +73,10 @@ typedef struct {
 #define SGFIM_F_WINDOWS_HORIZONTAL 0x10u /* sgfim_ring_mine_windows searches each task on horizontal
                                             item masks instead of vertical rows (slower; kept for
                                             comparison) */
+#define SGFIM_F_NO_PROJECTION 0x20u /* the miner searches every node on the whole database; by
+                                       default a root subtree is searched on its root item's
+                                       projected database once the data hold 131,072+ transactions */
+#define SGFIM_F_PROJECT 0x40u      /* project root subtrees whatever the size */
 
 /* Open a handle on a device.  Replaces the engines' process start-up
  * (kernel_bitmap.cu:796-800, AnytimeMining/kernel.cu:798-805). */

@@ -174,6 +174,49 @@ def test_cli_shims_results_files(tmp_path):
     assert len(a.arrays["runtimePerStage(s)"]) == 12
 
 
+@pytest.mark.parametrize("projection", [True, False])
+@pytest.mark.parametrize("n,sensors,bins,regimes,alpha,frac,seed", [
+    (100_000, 20, 8, 32, 0.2, 0.01, 0),
+    (50_000, 80, 8, 32, 0.2, 0.08, 1),
+    (20_000, 21, 6, 8, 0.3, 0.03, 2),
+    (3_000, 6, 4, 3, 0.3, 0.05, 3),
+])
+def test_projected_root_subtrees_match_oracle(projection, n, sensors, bins, regimes, alpha, frac, seed):
+    """Every root subtree searched on its root item's projected database (forced
+    here at sizes that would not project by default) gives the oracle's set, in
+    every frontier order and with few mask slots (head-row queries on the
+    projection)."""
+    from sgfim.engine import Engine
+    rows = datagen.regime_txns(n, sensors, bins, regimes, alpha, seed=seed)
+    rp, it = datagen.txns_to_csr(rows)
+    bm, _ = oracle.build_bitmaps(rp, it, sensors * bins)
+    thr = int(np.ceil(frac * n))
+    ref, _ = oracle.mine_fast(bm, n, thr)
+    want = {frozenset(s): c for s, c in ref}
+    for budget, wave in ((0, 0), (1 << 20, 5)):
+        with Engine(projection=projection, hbm_budget=budget, wave_nodes=wave) as eng:
+            eng.load_csr(rp, it)
+            for order in ("support", "support_desc"):
+                assert eng.mine(thr, order=order).as_dict() == want, (budget, wave, order)
+
+
+def test_projection_default_on_large_data_equals_whole_database():
+    """At 400,000 x 640 the miner projects by default; the search on the whole
+    database gives the same set.  (The number of nodes may differ: HUT tests a
+    node against the candidates emitted before its wave, and projected waves
+    group nodes differently.)"""
+    from sgfim.engine import Engine
+    rows = datagen.regime_txns(400_000, 80, 8, 32, 0.2, seed=5)
+    thr = int(np.ceil(0.05 * len(rows)))
+    out = {}
+    for projection in (None, False):
+        with Engine(projection=projection) as eng:
+            eng.load_rows(rows)
+            res = eng.mine(thr)
+            out[projection] = res.as_dict()
+    assert out[None] == out[False] and len(out[None]) > 1000
+
+
 @pytest.mark.parametrize("wave_nodes,floor", [(1, 0.08), (7, 0.05), (64, 0.02), (0, 0.02)])
 def test_mine_exact_under_mask_arena_pressure(wave_nodes, floor):
     """A 1 MiB budget leaves the miner ~100 tidset-mask slots, so most nodes

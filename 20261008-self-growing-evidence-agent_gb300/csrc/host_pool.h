@@ -1,0 +1,102 @@
+// host_pool.h -- a persistent pool of host threads for the miner's per-node
+// bookkeeping between device waves.
+//
+// run(n, fn) calls fn(lo, hi) on chunks of [0, n) taken from a shared counter
+// by the caller and the pool's threads, and returns when every chunk is done.
+// The threads are started on first use and sleep on a condition variable
+// between calls, so a wave costs two wake-ups, not thread creation.
+#pragma once
+
+#include <stdint.h>
+
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace sg {
+
+class HostPool {
+  public:
+    explicit HostPool(unsigned threads) : n_(std::max(1u, threads)) {}
+    HostPool(const HostPool &) = delete;
+    HostPool &operator=(const HostPool &) = delete;
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+    unsigned threads() const { return n_; }
+
+    // fn(lo, hi) over [0, n) in chunks of `chunk`; serial when n is at most one chunk
+    template <class F> void run(uint64_t n, uint64_t chunk, F &&fn) {
+        if (n == 0) return;
+        chunk = std::max<uint64_t>(chunk, 1);
+        if (n_ == 1 || n <= chunk) {
+            fn((uint64_t)0, n);
+            return;
+        }
+        if (th_.empty()) start();
+        job_ = [&fn](uint64_t lo, uint64_t hi) { fn(lo, hi); };
+        n_job_ = n;
+        chunk_ = chunk;
+        next_.store(0, std::memory_order_relaxed);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            pending_ = (unsigned)th_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+  private:
+    void start() {
+        th_.reserve(n_ - 1);
+        for (unsigned i = 1; i < n_; ++i) th_.emplace_back([this] { loop(); });
+    }
+    void work() {
+        for (;;) {
+            const uint64_t lo = next_.fetch_add(chunk_, std::memory_order_relaxed);
+            if (lo >= n_job_) return;
+            job_(lo, std::min(n_job_, lo + chunk_));
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+
+    const unsigned n_;
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    uint64_t gen_ = 0;
+    unsigned pending_ = 0;
+    bool stop_ = false;
+    std::function<void(uint64_t, uint64_t)> job_;
+    uint64_t n_job_ = 0, chunk_ = 1;
+    std::atomic<uint64_t> next_{0};
+};
+
+}  // namespace sg

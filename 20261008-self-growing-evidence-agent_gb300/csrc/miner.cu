@@ -9,11 +9,13 @@
 //   node (H, T):   s_e = sup(H u {e}) for e in T, counted on the device from H's
 //                  tidset mask (one batched launch per wave of nodes)
 //   PEP:           e with s_e == sup(H) joins H (same tidset)
-//   tail order:    the remaining frequent tail F sorted by ascending support
+//   tail order:    the remaining frequent tail F in the order's sequence
+//                  (ascending support in H's context by default)
 //   leaf:          F empty -> H is a candidate unless a pool member contains it
 //   HUT:           H u F contained in a pool member -> no new MFI below
 //   FHUT:          sup(H u F) >= thr -> H u F is the subtree's only candidate
-//   children:      H u {f_i} with tail f_{i+1..}, masks built on the device
+//   children:      H u {f_i} with tail f_{i+1..}, masks built on the device,
+//                  searched f_0 first
 //
 // The pool of candidates lives on the device as a vertical bitmap (one bit
 // per candidate in every item's row), so "is Q contained in a candidate" is an
@@ -32,9 +34,13 @@
 // subtree is left; a wave may hold nodes of several resident projections, and
 // its queries address rows through the slot of each node's projection.
 //
-// The order in which sibling subtrees are searched is a policy (canonical
-// ascending support, support descending, or the learned scorer); the tree,
-// every count and the final set do not depend on it.
+// The order of each node's extensions is a policy that shapes the tree (which
+// items each child's tail holds, so how soon HUT and FHUT prune) but never the
+// final set: canonical ascending support in the node's context; the
+// reference's plain order, one global order of descending item support
+// (kernel_bitmap.cu:276-283, exp_e6_cpuvec.py:65-69); or descending score of
+// the loaded scoring MLP.  Any order enumerates every frequent superset of H
+// inside F exactly once, and the pruning rules hold for any order.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -45,6 +51,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "host_pool.h"
 
 namespace sg {
 
@@ -62,7 +69,7 @@ constexpr uint32_t kDim = SGFIM_TRACE_DIM;
 
 struct MNode {
     std::vector<uint32_t> head;  // dense ids
-    std::vector<uint32_t> tail;  // dense ids, ascending support
+    std::vector<uint32_t> tail;  // dense ids, in the order's sequence
     uint32_t sup = 0;
     uint32_t slot = kNoSlot;     // tidset mask slot; kNoSlot = AND of head rows
     uint32_t id = 0;             // search-tree node id
@@ -177,6 +184,8 @@ class Miner {
     DevBuf &q_out_, &score_;
     HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
+    // per-node bookkeeping of a wave (PEP, extension order, candidates, children)
+    HostPool hp_{std::min(16u, std::max(1u, std::thread::hardware_concurrency()))};
     // vectors of finished nodes, reused for new children (no allocation per node once warm)
     std::vector<std::vector<uint32_t>> spare_;
     std::vector<uint64_t> cand_freq_;   // candidates holding each dense item (pool row density)
@@ -186,13 +195,14 @@ class Miner {
         spare_.pop_back();
         return v;
     }
-    double phase_[6] = {0, 0, 0, 0, 0, 0};   // see sgfim_result.phase_s
+    double phase_[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // see sgfim_result.phase_s
     // adds the wall time of f() to phase_[i]
     template <class F> void timed(int i, F &&f) {
         const auto a = Clock::now();
         f();
         phase_[i] += std::chrono::duration<double>(Clock::now() - a).count();
     }
+    void add_since(int i, Clock::time_point a) { phase_[i] += std::chrono::duration<double>(Clock::now() - a).count(); }
 
     double elapsed() const { return std::chrono::duration<double>(Clock::now() - t0_).count(); }
     uint32_t alloc_slot() {
@@ -206,7 +216,6 @@ class Miner {
     void run_tail_counts(const std::vector<uint64_t> &ptr, const std::vector<uint32_t> &items,
                          const std::vector<uint32_t> &slots, std::vector<uint32_t> &out);
     void pool_reserve(uint64_t members);
-    void emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node);
     void flush_pool(uint64_t from);
     void load_cooc();
     void features(const std::vector<uint32_t> &head, uint32_t head_sup, uint32_t e, uint32_t s, uint32_t pos,
@@ -285,19 +294,6 @@ void Miner::pool_reserve(uint64_t members) {
     pool_.ptr = np;
     pool_.bytes = (size_t)ds_.d * nw * 8;
     pool_words_ = nw;
-}
-
-void Miner::emit(const std::vector<uint32_t> &set, uint32_t sup, uint32_t node) {
-    const size_t at = citems_.size();
-    citems_.insert(citems_.end(), set.begin(), set.end());
-    std::sort(citems_.begin() + at, citems_.end());
-    cptr_.push_back(citems_.size());
-    csup_.push_back(sup);
-    ctime_.push_back(elapsed());
-    cexpanded_.push_back(nodes_);
-    cnode_.push_back(node);
-    ccheck_.push_back(pool_n_);
-    for (size_t k = at; k < citems_.size(); ++k) ++cand_freq_[citems_[k]];
 }
 
 // Append candidates [from, n) to the device pool (asynchronous; the next
@@ -480,13 +476,16 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     struct Work {
         std::vector<uint32_t> head;                    // after PEP
         std::vector<std::pair<uint32_t, uint32_t>> f;  // (support, item), ascending
-        int kind = 0;                                  // 0 leaf, 1 internal
+        std::vector<uint32_t> pq, fq;                  // pool query (rarest row first), FHUT query rows
+        int kind = 0;                                  // 0 leaf, 1 internal, 2 pruned or FHUT, 3 expands
+        int emit = 0;                                  // a candidate: head (leaf) or head u F (FHUT)
         size_t pool_q = 0, fhut_q = 0;
+        size_t e0 = 0, ei0 = 0;                        // its candidate's index and item offset in the wave
+        size_t feat0 = 0;                              // first feature row of its extensions
         size_t kid0 = 0, nkids = 0;                    // range in the wave's kid list
     };
     std::vector<Work> work;
     std::vector<MNode> kids;
-    std::vector<size_t> ord;
     std::vector<std::pair<uint32_t, uint32_t>> kid_src;  // (parent slot, added item)
     std::vector<uint32_t> child_slot;
 
@@ -579,47 +578,57 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             run_tail_counts(t_ptr, t_items, t_slot, counts);
             run_queries(qs, vrows_, vstride_, vwords_, vd_, QUERY_COUNT, counts_q);
         });
-        // ---- phase B: PEP, ordering, pool and FHUT queries
-        // Work records keep their vectors' capacity from wave to wave
+        // ---- phase B: PEP, extension order, pool and FHUT queries; each node on
+        // the host pool, then the query lists concatenated in wave order
+        auto t_exp = Clock::now();
         if (work.size() < wave.size()) work.resize(wave.size());
-        for (size_t i = 0; i < wave.size(); ++i) {
-            work[i].head.clear();
-            work[i].f.clear();
-            work[i].kind = 0;
-            work[i].pool_q = work[i].fhut_q = work[i].kid0 = work[i].nkids = 0;
-        }
+        hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                const MNode &nd = wave[i];
+                Work &wk = work[i];
+                wk.head.assign(nd.head.begin(), nd.head.end());
+                wk.f.clear();
+                wk.emit = 0;
+                wk.pool_q = wk.fhut_q = wk.feat0 = wk.kid0 = wk.nkids = 0;
+                const uint32_t *cs =
+                    (count_src[i].first == 0 ? counts.data() : counts_q.data()) + count_src[i].second;
+                for (size_t j = 0; j < nd.tail.size(); ++j) {
+                    const uint32_t s = cs[j];
+                    if (s < thr_) continue;
+                    if (s == nd.sup) wk.head.push_back(nd.tail[j]);
+                    else wk.f.emplace_back(s, nd.tail[j]);
+                }
+                std::sort(wk.f.begin(), wk.f.end());
+                wk.kind = wk.f.empty() ? 0 : 1;
+                // FHUT: the AND of F over a masked node's mask, else of head and F
+                wk.fq.clear();
+                if (wk.kind == 1) {
+                    const uint32_t off =
+                        (use_proj_ && nd.proj != kNoProj) ? (uint32_t)root_slot_[nd.proj] * ds_.d : 0u;
+                    if (nd.slot == kNoSlot)
+                        for (uint32_t h : wk.head) wk.fq.push_back(h + off);
+                    for (auto &pr : wk.f) wk.fq.push_back(pr.second + off);
+                }
+                // the pool query lists the rarest pool rows first: the device AND empties
+                // sooner and stops reading rows
+                wk.pq.assign(wk.head.begin(), wk.head.end());
+                for (auto &pr : wk.f) wk.pq.push_back(pr.second);
+                std::sort(wk.pq.begin(), wk.pq.end(),
+                          [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
+            }
+        });
         qpool.clear();
         qfhut.clear();
         for (size_t i = 0; i < wave.size(); ++i) {
-            MNode &nd = wave[i];
             Work &wk = work[i];
-            wk.head = nd.head;
-            const uint32_t *cs = (count_src[i].first == 0 ? counts.data() : counts_q.data()) + count_src[i].second;
-            for (size_t j = 0; j < nd.tail.size(); ++j) {
-                const uint32_t s = cs[j];
-                if (s < thr_) continue;
-                if (s == nd.sup) wk.head.push_back(nd.tail[j]);
-                else wk.f.emplace_back(s, nd.tail[j]);
-            }
-            std::sort(wk.f.begin(), wk.f.end());
-            tmp.assign(wk.head.begin(), wk.head.end());
-            for (auto &pr : wk.f) tmp.push_back(pr.second);
-            if (wk.f.empty()) {
-                wk.kind = 0;
-            } else {
-                // tmp = head, then F: the FHUT query of a masked node takes the F part
-                wk.kind = 1;
-                wk.fhut_q = qfhut.size();
-                if (nd.slot != kNoSlot) add_query(qfhut, nd, tmp.data() + wk.head.size(), wk.f.size(), nd.slot);
-                else add_query(qfhut, nd, tmp.data(), tmp.size(), kNoSlot);
-            }
-            // the pool query lists the rarest pool rows first: the device AND empties
-            // sooner and stops reading rows
-            std::sort(tmp.begin(), tmp.end(),
-                      [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
             wk.pool_q = qpool.size();
-            qpool.add(tmp.data(), tmp.size(), kNoSlot);
+            qpool.add(wk.pq.data(), wk.pq.size(), kNoSlot);
+            if (wk.kind == 1) {
+                wk.fhut_q = qfhut.size();
+                qfhut.add(wk.fq.data(), wk.fq.size(), wave[i].slot);
+            }
         }
+        add_since(6, t_exp);
         if (pool_n_ > 0) {
             const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
             timed(1, [&] { run_queries(qpool, pool_.as<uint64_t>(), pool_words_, pw, d, QUERY_ANY, pool_hit); });
@@ -627,55 +636,138 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             pool_hit.assign(qpool.size(), 0);
         }
         timed(2, [&] { run_queries(qfhut, vrows_, vstride_, vwords_, vd_, QUERY_COUNT, fhut_cnt); });
-        // ---- phase C: emit candidates, create children
+        // ---- phase C: leaf and FHUT candidates, HUT, expanding nodes
+        t_exp = Clock::now();
         const uint64_t pool_before = csup_.size();
-        kids.clear();
-        kid_src.clear();
-        wfeat.clear();
-        for (size_t i = 0; i < wave.size(); ++i) {
-            MNode &nd = wave[i];
-            Work &wk = work[i];
-            if (wk.kind == 0) {
-                if (!wk.head.empty() && pool_hit[wk.pool_q] == 0) emit(wk.head, nd.sup, nd.id);
-                continue;
-            }
-            if (pool_hit[wk.pool_q] != 0) continue;  // HUT
-            if (fhut_cnt[wk.fhut_q] >= thr_) {       // FHUT
-                tmp.assign(wk.head.begin(), wk.head.end());
-                for (auto &pr : wk.f) tmp.push_back(pr.second);
-                emit(tmp, fhut_cnt[wk.fhut_q], nd.id);
-                continue;
-            }
-            const size_t nf = wk.f.size();
-            wk.kid0 = kids.size();
-            wk.nkids = nf;
-            for (size_t j = 0; j < nf; ++j) {
-                MNode c;
-                c.head = take_spare();
-                c.tail = take_spare();
-                c.head.assign(wk.head.begin(), wk.head.end());
-                c.head.push_back(wk.f[j].second);
-                c.sup = wk.f[j].first;
-                c.tail.reserve(nf - j - 1);
-                for (size_t k = j + 1; k < nf; ++k) c.tail.push_back(wk.f[k].second);
-                c.id = (uint32_t)parent_.size();
-                c.proj = (use_proj_ && nd.proj == kNoProj) ? wk.f[j].second : nd.proj;
-                parent_.push_back(nd.id);
-                if (need_feat_) {
-                    float f[kDim];
-                    features(wk.head, nd.sup, wk.f[j].second, wk.f[j].first, (uint32_t)j, (uint32_t)nf, f);
-                    wfeat.insert(wfeat.end(), f, f + kDim);
-                    if (p_.record_trace) {
-                        tfeat_.insert(tfeat_.end(), f, f + kDim);
-                        tnode_.push_back(c.id);
-                    }
+        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                Work &wk = work[i];
+                if (wk.kind == 0) {
+                    wk.emit = !wk.head.empty() && pool_hit[wk.pool_q] == 0;
+                    continue;
                 }
-                kid_src.emplace_back(nd.slot, wk.f[j].second);
-                kids.push_back(std::move(c));
+                wk.kind = 2;
+                if (pool_hit[wk.pool_q] != 0) continue;  // HUT
+                if (fhut_cnt[wk.fhut_q] >= thr_) {       // FHUT: head u F is the subtree's candidate
+                    wk.emit = 1;
+                    continue;
+                }
+                wk.kind = 3;
+            }
+        });
+        // positions (wave order): candidates, their items, extensions (= children)
+        uint64_t n_emit = 0, n_emit_items = 0, n_ext = 0;
+        for (size_t i = 0; i < wave.size(); ++i) {
+            Work &wk = work[i];
+            if (wk.emit) {
+                wk.e0 = n_emit++;
+                wk.ei0 = n_emit_items;
+                n_emit_items += wk.head.size() + (wk.kind == 2 ? wk.f.size() : 0);
+            }
+            if (wk.kind == 3) {
+                wk.feat0 = wk.kid0 = n_ext;
+                wk.nkids = wk.f.size();
+                n_ext += wk.f.size();
             }
         }
-        // learned order: score every child of the wave in one launch
-        if (p_.order == SGFIM_ORDER_LEARNED) timed(4, [&] { score(wfeat, kids.size(), wscore); });
+        if (n_emit) {
+            const uint64_t c0 = csup_.size(), it0 = citems_.size();
+            citems_.resize(it0 + n_emit_items);
+            cptr_.resize(c0 + 1 + n_emit);
+            csup_.resize(c0 + n_emit);
+            cnode_.resize(c0 + n_emit);
+            hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t i = lo; i < hi; ++i) {
+                    const Work &wk = work[i];
+                    if (!wk.emit) continue;
+                    uint32_t *dst = citems_.data() + it0 + wk.ei0;
+                    uint32_t *e = std::copy(wk.head.begin(), wk.head.end(), dst);
+                    if (wk.kind == 2)
+                        for (auto &pr : wk.f) *e++ = pr.second;
+                    std::sort(dst, e);
+                    cptr_[c0 + 1 + wk.e0] = (uint64_t)(e - citems_.data());
+                    csup_[c0 + wk.e0] = wk.kind == 2 ? fhut_cnt[wk.fhut_q] : wave[i].sup;
+                    cnode_[c0 + wk.e0] = wave[i].id;
+                }
+            });
+            ctime_.resize(c0 + n_emit, elapsed());
+            cexpanded_.resize(c0 + n_emit, nodes_);
+            ccheck_.resize(c0 + n_emit, pool_n_);
+            for (uint64_t k = it0; k < citems_.size(); ++k) ++cand_freq_[citems_[k]];
+        }
+        // features of the expanding nodes' extensions (F in ascending support; the
+        // position feature is that rank)
+        if (need_feat_) {
+            wfeat.resize(n_ext * kDim);
+            hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t i = lo; i < hi; ++i) {
+                    const Work &wk = work[i];
+                    if (wk.kind != 3) continue;
+                    const size_t nf = wk.f.size();
+                    for (size_t j = 0; j < nf; ++j)
+                        features(wk.head, wave[i].sup, wk.f[j].second, wk.f[j].first, (uint32_t)j, (uint32_t)nf,
+                                 wfeat.data() + (wk.feat0 + j) * kDim);
+                }
+            });
+        }
+        add_since(6, t_exp);
+        // learned order: score every extension of the wave in one launch
+        if (p_.order == SGFIM_ORDER_LEARNED) timed(4, [&] { score(wfeat, n_ext, wscore); });
+        t_exp = Clock::now();
+        // children in the order's sequence: the p-th extension's tail is the
+        // extensions after it, and the first is searched first
+        kids.clear();
+        kids.resize(n_ext);
+        kid_src.resize(n_ext);
+        for (MNode &c : kids) {
+            c.head = take_spare();
+            c.tail = take_spare();
+        }
+        const uint64_t id0 = parent_.size(), tr0 = tnode_.size();
+        parent_.resize(id0 + n_ext);
+        if (p_.record_trace) {
+            tfeat_.resize((tr0 + n_ext) * kDim);
+            tnode_.resize(tr0 + n_ext);
+        }
+        hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+            std::vector<uint32_t> rank;
+            for (uint64_t i = lo; i < hi; ++i) {
+                const MNode &nd = wave[i];
+                const Work &wk = work[i];
+                if (wk.kind != 3) continue;
+                const size_t nf = wk.f.size();
+                rank.resize(nf);
+                std::iota(rank.begin(), rank.end(), (uint32_t)0);
+                if (p_.order == SGFIM_ORDER_SUPPORT_DESC) {
+                    std::sort(rank.begin(), rank.end(), [&](uint32_t a, uint32_t b) {
+                        const uint32_t x = wk.f[a].second, y = wk.f[b].second;
+                        return ds_.sup[x] != ds_.sup[y] ? ds_.sup[x] > ds_.sup[y] : x < y;
+                    });
+                } else if (p_.order == SGFIM_ORDER_LEARNED) {
+                    const float *sc = wscore.data() + wk.feat0;
+                    std::stable_sort(rank.begin(), rank.end(), [&](uint32_t a, uint32_t b) { return sc[a] > sc[b]; });
+                }
+                for (size_t p = 0; p < nf; ++p) {
+                    const uint32_t j = rank[p];
+                    const uint64_t k = wk.kid0 + p;
+                    MNode &c = kids[k];
+                    c.head.assign(wk.head.begin(), wk.head.end());
+                    c.head.push_back(wk.f[j].second);
+                    c.sup = wk.f[j].first;
+                    c.tail.resize(nf - p - 1);
+                    for (size_t q = p + 1; q < nf; ++q) c.tail[q - p - 1] = wk.f[rank[q]].second;
+                    c.id = (uint32_t)(id0 + k);
+                    c.proj = (use_proj_ && nd.proj == kNoProj) ? wk.f[j].second : nd.proj;
+                    parent_[id0 + k] = nd.id;
+                    if (p_.record_trace) {
+                        std::copy_n(wfeat.data() + (wk.feat0 + j) * kDim, kDim, tfeat_.data() + (tr0 + k) * kDim);
+                        tnode_[tr0 + k] = c.id;
+                    }
+                    kid_src[k] = {nd.slot, wk.f[j].second};
+                }
+            }
+        });
+        add_since(6, t_exp);
         // child masks for the children searched next: mask(child) = mask(parent) & row(e)
         qchild.clear();
         child_slot.clear();
@@ -703,21 +795,15 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                                dcs, (uint32_t)n, st, h_->n_sm);
             ++launches_;
         }
-        // sibling visiting order
+        // the stack is LIFO: push in reverse so that the wave's first node's first
+        // child is popped first
+        t_exp = Clock::now();
         for (size_t i = wave.size(); i-- > 0;) {
-            // stack is LIFO: nodes pushed later are popped first; keep wave order
             Work &wk = work[i];
-            if (wk.kind == 0 || wk.nkids == 0) continue;
-            ord.resize(wk.nkids);
-            std::iota(ord.begin(), ord.end(), wk.kid0);
-            if (p_.order == SGFIM_ORDER_SUPPORT_DESC) {
-                std::reverse(ord.begin(), ord.end());
-            } else if (p_.order == SGFIM_ORDER_LEARNED) {
-                std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return wscore[a] > wscore[b]; });
-            }
-            for (size_t j = ord.size(); j-- > 0;) {
-                if (use_proj_ && kids[ord[j]].proj != kNoProj) ++live_[kids[ord[j]].proj];
-                stack.push_back(std::move(kids[ord[j]]));
+            if (wk.kind != 3) continue;
+            for (size_t j = wk.kid0 + wk.nkids; j-- > wk.kid0;) {
+                if (use_proj_ && kids[j].proj != kNoProj) ++live_[kids[j].proj];
+                stack.push_back(std::move(kids[j]));
             }
         }
         // parents' masks are no longer needed once the child-mask kernel ran (stream order)
@@ -725,6 +811,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             if (nd.slot != kNoSlot) free_slots_.push_back(nd.slot);
             if (use_proj_ && nd.proj != kNoProj) --live_[nd.proj];
         }
+        add_since(6, t_exp);
         flush_pool(pool_before);
         // ---- checkpoints, limits
         const double el = elapsed();
@@ -787,6 +874,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
 }
 
 int Miner::finish(sgfim_result **out) {
+    const auto t_fin = Clock::now();
+    const double filter0 = phase_[3];
     const uint64_t n = csup_.size();
     // maximality filter: a candidate was already tested against every member
     // that existed when it was found, so only later members (its own bit
@@ -936,8 +1025,10 @@ int Miner::finish(sgfim_result **out) {
     r->waves = waves_;
     r->kernel_launches = launches_;
     r->candidates = n;
-    phase_[5] = r->elapsed_s - (phase_[0] + phase_[1] + phase_[2] + phase_[3] + phase_[4]);
-    for (int i = 0; i < 6; ++i) r->phase_s[i] = phase_[i];
+    add_since(7, t_fin);
+    phase_[7] -= phase_[3] - filter0;
+    phase_[5] = r->elapsed_s - (phase_[0] + phase_[1] + phase_[2] + phase_[3] + phase_[4] + phase_[6] + phase_[7]);
+    for (int i = 0; i < 8; ++i) r->phase_s[i] = phase_[i];
     *out = r;
     return SGFIM_OK;
 }

@@ -45,7 +45,7 @@ class Result(C.Structure):
                 ("elapsed_s", C.c_double), ("preprocess_s", C.c_double), ("nodes", C.c_uint64),
                 ("waves", C.c_uint64), ("kernel_launches", C.c_uint64), ("candidates", C.c_uint64),
                 ("trace_n", C.c_uint64), ("trace_dim", C.c_uint32), ("trace_features", f32p),
-                ("trace_labels", C.POINTER(C.c_uint8)), ("phase_s", C.c_double * 6), ("emit_node", u64p)]
+                ("trace_labels", C.POINTER(C.c_uint8)), ("phase_s", C.c_double * 8), ("emit_node", u64p)]
 
 
 class MineParams(C.Structure):

@@ -46,7 +46,7 @@ class MineResult:
         self.waves = int(r.waves)
         self.kernel_launches = int(r.kernel_launches)
         self.candidates = int(r.candidates)
-        self.phase_s = dict(zip(("counts", "pool", "fhut", "final_filter", "scoring", "other"),
+        self.phase_s = dict(zip(("counts", "pool", "fhut", "final_filter", "scoring", "other", "expand", "assemble"),
                                 (float(x) for x in r.phase_s)))
         tn, td = int(r.trace_n), int(r.trace_dim)
         if tn:

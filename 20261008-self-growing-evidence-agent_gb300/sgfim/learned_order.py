@@ -1,8 +1,19 @@
-"""Learned frontier ordering: traces -> training -> held-out evaluation.
+"""Learned extension ordering: traces -> training -> held-out evaluation.
+
+The order of each search node's frequent extensions shapes the tree: child
+H u {f_i} gets the tail f_{i+1..}, so the extensions placed first carry the
+largest tails, and HUT/FHUT prune later children against what the earlier
+ones found.  Three orders, every final MFI set identical:
+
+* plain (``support_desc``): the reference's order, one global order of
+  descending item support (kernel_bitmap.cu:276-283, exp_e6_cpuvec.py:65-69);
+* canonical (``support``): ascending support in the node's context;
+* learned: descending score of the scoring MLP, which predicts P(the child's
+  subtree emits a final MFI) from the extension's features.
 
 The committed scorer (sgfim/data/scorer_weights.npz) was trained by the
-project's own kernels on traces of 200 seeded 20,000-transaction streams at a
-6% floor:
+project's own kernels on traces of the scorer-free miner (canonical order) on
+200 seeded 20,000-transaction streams at a 6% floor:
 
     python -m sgfim.learned_order --train-seeds 200 --n-txn 20000 --floor 0.06 \
         --eval-seeds 20 --eval-n-txn 2000000 --eval-floor 0.03 \
@@ -10,14 +21,8 @@ project's own kernels on traces of 200 seeded 20,000-transaction streams at a
 
 Workload family: the anytime-2m generator (80 sensors x 8 bins = 640 items,
 one item per sensor per transaction, 32 latent regimes, Dirichlet(0.2) bin
-probabilities), with a per-stream seed.  The plain miner (siblings visited by
-descending support, the reference's frequency order) records one trace row
-per created child; the MLP learns P(child subtree emits a final MFI).  The
-learned order then visits siblings by descending score.  Every run's final
-MFI set is compared with the plain run's: the order may only change when
-MFIs are emitted, never which.
-
-    python -m sgfim.learned_order --train-seeds 200 --eval-seeds 20 --n-txn 20000 --floor 0.06
+probabilities), with a per-stream seed.  Every run's final MFI set is
+compared with the plain run's.
 """
 from __future__ import annotations
 
@@ -40,7 +45,7 @@ def stream_rows(seed, n_txn):
                                FAMILY["alpha_bin"], seed=seed)
 
 
-def collect_traces(eng, seeds, n_txn, floor, order="support_desc"):
+def collect_traces(eng, seeds, n_txn, floor, order="support"):
     X, Y, stats = [], [], []
     for s in seeds:
         eng.load_rows(stream_rows(s, n_txn))
@@ -82,12 +87,10 @@ def evaluate(eng, seeds, n_txn, floor, reps=1):
 
 
 def summarize(rows):
-    """Learned / support-descending ratios (geomean and median over seeds) of the
-    time and of the search nodes to each coverage level, and the same for the
-    canonical order (lowest-support sibling first)."""
-    out = {"identical_all": all(r["identical"] for r in rows), "seeds": len(rows),
-           "nodes_equal_all_orders": all(r["learned"]["nodes"] == r["support_desc"]["nodes"] == r["support"]["nodes"]
-                                         for r in rows)}
+    """Learned / plain (support-descending) ratios, geomean and median over seeds,
+    of the time and of the search nodes to each coverage level, and the same
+    for the canonical order."""
+    out = {"identical_all": all(r["identical"] for r in rows), "seeds": len(rows)}
     for order in ("learned", "support"):
         for key in ("t50", "t90", "t95", "n50", "n90", "n95", "total_s", "nodes"):
             ratio = [r[order][key] / max(r["support_desc"][key], 1e-9) for r in rows]
@@ -104,8 +107,8 @@ def load_weights(eng, path):
 
 def evaluate_committed(weights_path, n_seeds=3, n_txn=2_000_000, floor=0.03, first_seed=5010):
     """Held-out streams of the anytime-2m family with committed scorer weights:
-    coverage times and nodes of the learned, canonical and support-descending
-    orders, final sets compared."""
+    coverage times and nodes of the learned, canonical and plain orders, final
+    sets compared."""
     with Engine() as eng:
         load_weights(eng, weights_path)
         rows = evaluate(eng, range(first_seed, first_seed + n_seeds), n_txn, floor)

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define SGFIM_ABI_VERSION 2
+#define SGFIM_ABI_VERSION 3
 
 enum {
     SGFIM_OK = 0,
@@ -278,8 +278,11 @@ typedef struct {
     /* wall time of the search phases (each device phase ends in a stream
      * synchronisation, so device time of asynchronous launches is charged to
      * the next phase): [0] extension counts, [1] pool (HUT / leaf) queries,
-     * [2] FHUT counts, [3] final maximality filter, [4] scoring, [5] the rest */
-    double phase_s[6];
+     * [2] FHUT counts, [3] final maximality filter, [4] scoring, [5] the rest
+     * (wave assembly, staging, launches, checkpoints), [6] host expansion (PEP,
+     * extension order, candidates, children), [7] result assembly after the
+     * search */
+    double phase_s[8];
     uint64_t *emit_node;     /* search nodes expanded when each set was emitted (a clock-free
                                 measure of how early the search order reaches it) */
 } sgfim_result;
@@ -291,13 +294,14 @@ typedef struct {
 #define SGFIM_ROOTS_LIST 1    /* the ids in `roots` (AnyFIM stage k: the top-k ids, AnytimeMining/kernel.cu:850-859) */
 #define SGFIM_ROOTS_MINCOUNT 2 /* ids with count >= root_min_count (TensorFIM: count/n > thr, kernel_bmma.cu:1199,1224-1233) */
 
-/* Frontier orders: the order in which sibling subtrees are searched.  The
- * tree itself (every node's tail: the frequent extensions of higher support)
- * and the final result never change; only the emission order does (node counts
- * are the same in every order, at every wave size). */
-#define SGFIM_ORDER_SUPPORT 0      /* canonical: lowest-support sibling first */
-#define SGFIM_ORDER_LEARNED 1      /* highest score of the loaded scoring MLP first */
-#define SGFIM_ORDER_SUPPORT_DESC 2 /* highest-support sibling first (the reference's frequency order) */
+/* Extension orders: the sequence of each search node's frequent extensions
+ * f_0, f_1, ...  Child H u {f_i} gets the tail f_{i+1..} and f_0 is searched
+ * first, so the order shapes the tree (how soon HUT/FHUT prune) and the
+ * emission times; the final result never changes. */
+#define SGFIM_ORDER_SUPPORT 0      /* canonical: ascending support in the node's context (ties: id) */
+#define SGFIM_ORDER_LEARNED 1      /* descending score of the loaded scoring MLP (ties: canonical) */
+#define SGFIM_ORDER_SUPPORT_DESC 2 /* plain: one global order, descending item support, ties ascending id
+                                      (the reference's frequency order, kernel_bitmap.cu:276-283) */
 
 typedef struct {
     uint32_t min_count;       /* absolute support threshold (>= 1) */

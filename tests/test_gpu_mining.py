@@ -129,8 +129,8 @@ def test_anytime_checkpoints(engine):
 
 
 def test_orders_give_identical_sets_and_traces(engine):
-    """Frontier orders change only the emission order; traces label the nodes on
-    the path to every final MFI."""
+    """Extension orders change the tree and the emission order, never the final
+    set; traces label the nodes on the path to every final MFI."""
     rows = datagen.regime_txns(40_000, 30, 8, 32, 0.2, seed=13)
     engine.load_rows(rows)
     thr = int(0.03 * 40_000)

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(L, s), f"libsgfim.so does not export {s}"
     assert set(syms) <= set(_lib.SIGNATURES), "ctypes binding misses a declared symbol"
-    assert L.sgfim_abi_version() == 2
+    assert L.sgfim_abi_version() == 3
 
 
 def test_open_without_gpu_returns_error_code():

@@ -126,8 +126,11 @@ void launch_projection(const uint64_t *rows, uint64_t stride, uint64_t n_words, 
 void launch_child_masks(uint64_t *arena, uint64_t arena_stride, uint64_t n_words, const uint64_t *rows,
                         uint64_t row_stride, const uint64_t *ptr, const uint32_t *items, const uint32_t *parent_slot,
                         const uint32_t *child_slot, uint32_t n, cudaStream_t st, int n_sm);
+// Sets the bit of member m (first_member + s, or set_col[s] when given) in the
+// pool row of every item of set s.
 void launch_pool_append(uint64_t *pool_rows, uint64_t pool_stride, const uint64_t *set_ptr,
-                        const uint32_t *set_items, uint64_t first_member, uint32_t n_sets, cudaStream_t st);
+                        const uint32_t *set_items, uint64_t first_member, uint32_t n_sets, cudaStream_t st,
+                        const uint64_t *set_col = nullptr);
 
 // Co-occurrence (d x d) over the bitmap rows.
 int cooc_device(const uint64_t *bitmaps, uint32_t d, uint64_t n_words, uint64_t row_stride, uint32_t *out,

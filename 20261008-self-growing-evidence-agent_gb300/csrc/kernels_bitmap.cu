@@ -1047,20 +1047,20 @@ void launch_child_masks(uint64_t *arena, uint64_t arena_stride, uint64_t n_words
 
 __global__ void pool_append_kernel(unsigned long long *__restrict__ pool, uint64_t pstride,
                                    const uint64_t *__restrict__ set_ptr, const uint32_t *__restrict__ set_items,
-                                   uint64_t first, uint32_t n_sets) {
+                                   uint64_t first, uint32_t n_sets, const uint64_t *__restrict__ set_col) {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_sets; s += gridDim.x * blockDim.x) {
-        const uint64_t m = first + s;
+        const uint64_t m = set_col ? set_col[s] : first + s;
         for (uint64_t i = set_ptr[s]; i < set_ptr[s + 1]; ++i)
             atomicOr(&pool[(uint64_t)set_items[i] * pstride + (m >> 6)], 1ull << (m & 63));
     }
 }
 
 void launch_pool_append(uint64_t *pool_rows, uint64_t pool_stride, const uint64_t *set_ptr, const uint32_t *set_items,
-                        uint64_t first_member, uint32_t n_sets, cudaStream_t st) {
+                        uint64_t first_member, uint32_t n_sets, cudaStream_t st, const uint64_t *set_col) {
     if (n_sets == 0) return;
     const unsigned blocks = std::min<unsigned>((n_sets + 255) / 256, 1024);
     pool_append_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<unsigned long long *>(pool_rows), pool_stride,
-                                               set_ptr, set_items, first_member, n_sets);
+                                               set_ptr, set_items, first_member, n_sets, set_col);
     SG_CUDA_TRY(cudaGetLastError());
 }
 

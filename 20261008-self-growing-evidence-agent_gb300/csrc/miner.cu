@@ -164,6 +164,16 @@ class Miner {
     DevBuf &pool_;
     uint64_t pool_words_ = 0;
     uint64_t pool_n_ = 0;
+    // slot pools: for each resident projection, the candidates that hold its root
+    // item (slot p's row e is row p*d + e).  Every node of a root subtree holds
+    // the root item, so only those candidates can contain its HUT and leaf
+    // queries, which read the slot pool instead of the whole pool.
+    bool use_spool_ = false;
+    uint64_t spool_words_ = 0;            // words per row
+    std::vector<uint64_t> spool_n_;       // candidates in each slot's pool
+    void spool_reserve(uint64_t members);
+    std::vector<uint64_t> sp_ptr_, sp_cols_;
+    std::vector<uint32_t> sp_items_;
     // candidates (host)
     std::vector<uint64_t> cptr_{0};
     std::vector<uint32_t> citems_;
@@ -296,6 +306,34 @@ void Miner::pool_reserve(uint64_t members) {
     pool_words_ = nw;
 }
 
+// Grow every slot pool's rows to hold `members` candidates (rows copied over;
+// the first use in a call adopts the workspace buffer, whose slots are cleared
+// when they are built).
+void Miner::spool_reserve(uint64_t members) {
+    // at least two words per row, also for no members: a slot is cleared over
+    // the row width when it is built, so the width must exist from the first build
+    const uint64_t need = std::max<uint64_t>(2, ((members + 63) / 64 + 1) & ~1ull);
+    if (need <= spool_words_) return;
+    const uint64_t rows = (uint64_t)n_proj_slots_ * ds_.d;
+    if (spool_words_ == 0 && w_.spool.bytes >= rows * need * 8) {
+        spool_words_ = (w_.spool.bytes / (rows * 8)) & ~1ull;
+        return;
+    }
+    uint64_t nw = std::max<uint64_t>(need, std::max<uint64_t>(spool_words_ * 2, 1024));
+    nw = (nw + 1) & ~1ull;
+    void *np = nullptr;
+    SG_CUDA_TRY(cudaMalloc(&np, rows * nw * 8));
+    SG_CUDA_TRY(cudaMemsetAsync(np, 0, rows * nw * 8, h_->stream));
+    if (w_.spool.ptr && spool_words_)
+        SG_CUDA_TRY(cudaMemcpy2DAsync(np, nw * 8, w_.spool.ptr, spool_words_ * 8, spool_words_ * 8, rows,
+                                      cudaMemcpyDeviceToDevice, h_->stream));
+    SG_CUDA_TRY(cudaStreamSynchronize(h_->stream));
+    w_.spool.release();
+    w_.spool.ptr = np;
+    w_.spool.bytes = rows * nw * 8;
+    spool_words_ = nw;
+}
+
 // Append candidates [from, n) to the device pool (asynchronous; the next
 // query synchronises the stream before the staging buffers are reused).
 void Miner::flush_pool(uint64_t from) {
@@ -310,6 +348,27 @@ void Miner::flush_pool(uint64_t from) {
     launch_pool_append(pool_.as<uint64_t>(), pool_words_, dp, di, from, cnt, h_->stream);
     ++launches_;
     pool_n_ = n;
+    if (!use_spool_) return;
+    // each new candidate also joins the pool of every resident slot whose root it holds
+    sp_ptr_.assign(1, 0);
+    sp_items_.clear();
+    sp_cols_.clear();
+    for (uint64_t c = from; c < n; ++c) {
+        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) {
+            const int32_t p = root_slot_[citems_[k]];
+            if (p < 0) continue;
+            const uint32_t off = (uint32_t)p * ds_.d;
+            for (uint64_t j = cptr_[c]; j < cptr_[c + 1]; ++j) sp_items_.push_back(citems_[j] + off);
+            sp_ptr_.push_back(sp_items_.size());
+            sp_cols_.push_back(spool_n_[p]++);
+        }
+    }
+    if (sp_cols_.empty()) return;
+    spool_reserve(*std::max_element(spool_n_.begin(), spool_n_.end()));
+    launch_pool_append(w_.spool.as<uint64_t>(), spool_words_, w_.s_ptr.put(sp_ptr_.data(), sp_ptr_.size(), h_->stream),
+                       w_.s_items.put(sp_items_.data(), sp_items_.size(), h_->stream), 0, (uint32_t)sp_cols_.size(),
+                       h_->stream, w_.s_cols.put(sp_cols_.data(), sp_cols_.size(), h_->stream));
+    ++launches_;
 }
 
 void Miner::load_cooc() {
@@ -392,6 +451,18 @@ bool Miner::make_resident(const MNode &nd) {
                       proj_stride_, proj_stride_, ds_.d, st, h_->n_sm);
     launches_ += 2;
     ++projections_;
+    if (use_spool_) {
+        // the pool projected on r's pool row: every candidate so far (all are in the
+        // device pool: the previous wave flushed them) that holds r
+        spool_reserve(cand_freq_[r]);
+        const uint64_t pw = pool_n_ ? ((pool_n_ + 63) / 64 + 1) & ~1ull : 0;
+        w_.pofs.reserve(std::max<uint64_t>(pw, 1) * 4, st);
+        launch_projection(pool_.as<uint64_t>(), pool_words_, pw, r, ditems, (uint32_t)items.size(),
+                          w_.pofs.as<uint32_t>(), w_.spool.as<uint64_t>() + (uint64_t)slot * ds_.d * spool_words_,
+                          spool_words_, spool_words_, ds_.d, st, h_->n_sm);
+        launches_ += 2;
+        spool_n_[slot] = cand_freq_[r];
+    }
     slot_root_[slot] = r;
     root_slot_[r] = slot;
     wp_[r] = ((ds_.sup[r] + 63) / 64 + 1) & ~1ull;
@@ -438,6 +509,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         root_slot_.assign(d, -1);
         live_.assign(d, 0);
         wp_.assign(d, 0);
+        use_spool_ = true;
+        spool_n_.assign(n_proj_slots_, 0);
     }
     // mask arena
     slot_words_ = use_proj_ ? proj_stride_ : ds_.stride;
@@ -615,10 +688,16 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 for (auto &pr : wk.f) wk.pq.push_back(pr.second);
                 std::sort(wk.pq.begin(), wk.pq.end(),
                           [&](uint32_t x, uint32_t y) { return cand_freq_[x] < cand_freq_[y]; });
+                if (use_spool_ && nd.proj != kNoProj) {
+                    const uint32_t off = (uint32_t)root_slot_[nd.proj] * ds_.d;
+                    for (uint32_t &x : wk.pq) x += off;
+                }
             }
         });
         qpool.clear();
         qfhut.clear();
+        const bool slot_pools = use_spool_ && !wave_global;
+        uint64_t spool_max = 0;   // candidates in the largest slot pool the wave reads
         for (size_t i = 0; i < wave.size(); ++i) {
             Work &wk = work[i];
             wk.pool_q = qpool.size();
@@ -627,9 +706,15 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 wk.fhut_q = qfhut.size();
                 qfhut.add(wk.fq.data(), wk.fq.size(), wave[i].slot);
             }
+            if (slot_pools) spool_max = std::max(spool_max, spool_n_[root_slot_[wave[i].proj]]);
         }
         add_since(6, t_exp);
-        if (pool_n_ > 0) {
+        if (slot_pools && spool_max > 0) {
+            const uint64_t pw = ((spool_max + 63) / 64 + 1) & ~1ull;
+            timed(1, [&] {
+                run_queries(qpool, w_.spool.as<uint64_t>(), spool_words_, pw, n_proj_slots_ * d, QUERY_ANY, pool_hit);
+            });
+        } else if (!slot_pools && pool_n_ > 0) {
             const uint64_t pw = ((pool_n_ + 63) / 64 + 1) & ~1ull;
             timed(1, [&] { run_queries(qpool, pool_.as<uint64_t>(), pool_words_, pw, d, QUERY_ANY, pool_hit); });
         } else {

@@ -172,7 +172,7 @@ class Miner {
     uint64_t spool_words_ = 0;            // words per row
     std::vector<uint64_t> spool_n_;       // candidates in each slot's pool
     void spool_reserve(uint64_t members);
-    std::vector<uint64_t> sp_ptr_, sp_cols_;
+    std::vector<uint64_t> sp_ptr_, sp_cols_, sp_cnt_, sp_io_;
     std::vector<uint32_t> sp_items_;
     // candidates (host)
     std::vector<uint64_t> cptr_{0};
@@ -199,12 +199,6 @@ class Miner {
     // vectors of finished nodes, reused for new children (no allocation per node once warm)
     std::vector<std::vector<uint32_t>> spare_;
     std::vector<uint64_t> cand_freq_;   // candidates holding each dense item (pool row density)
-    std::vector<uint32_t> take_spare() {
-        if (spare_.empty()) return {};
-        std::vector<uint32_t> v = std::move(spare_.back());
-        spare_.pop_back();
-        return v;
-    }
     double phase_[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // see sgfim_result.phase_s
     // adds the wall time of f() to phase_[i]
     template <class F> void timed(int i, F &&f) {
@@ -349,21 +343,44 @@ void Miner::flush_pool(uint64_t from) {
     ++launches_;
     pool_n_ = n;
     if (!use_spool_) return;
-    // each new candidate also joins the pool of every resident slot whose root it holds
-    sp_ptr_.assign(1, 0);
-    sp_items_.clear();
-    sp_cols_.clear();
-    for (uint64_t c = from; c < n; ++c) {
-        for (uint64_t k = cptr_[c]; k < cptr_[c + 1]; ++k) {
-            const int32_t p = root_slot_[citems_[k]];
-            if (p < 0) continue;
-            const uint32_t off = (uint32_t)p * ds_.d;
-            for (uint64_t j = cptr_[c]; j < cptr_[c + 1]; ++j) sp_items_.push_back(citems_[j] + off);
-            sp_ptr_.push_back(sp_items_.size());
-            sp_cols_.push_back(spool_n_[p]++);
+    // each new candidate also joins the pool of every resident slot whose root it
+    // holds: entries counted per candidate, positioned, then written in parallel
+    // (a slot's columns are taken from its counter, in any order: a slot pool is a set)
+    const uint64_t nn = n - from;
+    sp_cnt_.assign(nn + 1, 0);
+    hp_.run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            uint64_t k = 0;
+            for (uint64_t j = cptr_[from + i]; j < cptr_[from + i + 1]; ++j) k += root_slot_[citems_[j]] >= 0;
+            sp_cnt_[i + 1] = k;
         }
+    });
+    sp_io_.resize(nn + 1);
+    sp_io_[0] = 0;
+    for (uint64_t i = 0; i < nn; ++i) {
+        sp_io_[i + 1] = sp_io_[i] + sp_cnt_[i + 1] * (cptr_[from + i + 1] - cptr_[from + i]);
+        sp_cnt_[i + 1] += sp_cnt_[i];
     }
-    if (sp_cols_.empty()) return;
+    const uint64_t n_ent = sp_cnt_[nn];
+    if (n_ent == 0) return;
+    sp_items_.resize(sp_io_[nn]);
+    sp_ptr_.resize(n_ent + 1);
+    sp_cols_.resize(n_ent);
+    sp_ptr_[n_ent] = sp_io_[nn];
+    hp_.run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            const uint64_t a = cptr_[from + i], b = cptr_[from + i + 1];
+            uint64_t e = sp_cnt_[i], at = sp_io_[i];
+            for (uint64_t j = a; j < b; ++j) {
+                const int32_t p = root_slot_[citems_[j]];
+                if (p < 0) continue;
+                const uint32_t off = (uint32_t)p * ds_.d;
+                sp_ptr_[e] = at;
+                for (uint64_t q = a; q < b; ++q) sp_items_[at++] = citems_[q] + off;
+                sp_cols_[e++] = __atomic_fetch_add(&spool_n_[p], (uint64_t)1, __ATOMIC_RELAXED);
+            }
+        }
+    });
     spool_reserve(*std::max_element(spool_n_.begin(), spool_n_.end()));
     launch_pool_append(w_.spool.as<uint64_t>(), spool_words_, w_.s_ptr.put(sp_ptr_.data(), sp_ptr_.size(), h_->stream),
                        w_.s_items.put(sp_items_.data(), sp_items_.size(), h_->stream), 0, (uint32_t)sp_cols_.size(),
@@ -552,7 +569,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         std::vector<uint32_t> pq, fq;                  // pool query (rarest row first), FHUT query rows
         int kind = 0;                                  // 0 leaf, 1 internal, 2 pruned or FHUT, 3 expands
         int emit = 0;                                  // a candidate: head (leaf) or head u F (FHUT)
-        size_t pool_q = 0, fhut_q = 0;
+        size_t pool_q = 0, fhut_q = 0, fi0 = 0;        // its queries; fi0: its FHUT rows' offset
         size_t e0 = 0, ei0 = 0;                        // its candidate's index and item offset in the wave
         size_t feat0 = 0;                              // first feature row of its extensions
         size_t kid0 = 0, nkids = 0;                    // range in the wave's kid list
@@ -565,9 +582,17 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     while (!stack.empty()) {
         // ---- pop a wave
         // the previous wave's nodes are done: keep their vectors for the next children
-        for (MNode &nd : wave) {
-            if (nd.head.capacity()) { nd.head.clear(); spare_.push_back(std::move(nd.head)); }
-            if (nd.tail.capacity()) { nd.tail.clear(); spare_.push_back(std::move(nd.tail)); }
+        {
+            const size_t s0 = spare_.size();
+            spare_.resize(s0 + 2 * wave.size());
+            hp_.run(wave.size(), 2048, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t i = lo; i < hi; ++i) {
+                    wave[i].head.clear();
+                    wave[i].tail.clear();
+                    spare_[s0 + 2 * i] = std::move(wave[i].head);
+                    spare_[s0 + 2 * i + 1] = std::move(wave[i].tail);
+                }
+            });
         }
         wave.clear();
         uint64_t nq = 0;
@@ -625,18 +650,19 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         // ---- phase A: s_e for every tail item (nodes with a mask: one record per node;
         // nodes without one, created while the arena was full: a query per item)
+        // (positions in wave order here, the masked nodes' tail rows copied in parallel below)
         qs.clear();
         t_ptr.assign(1, 0);
-        t_items.clear();
         t_slot.clear();
         count_src.resize(wave.size());
+        uint64_t n_ti = 0;
         for (size_t i = 0; i < wave.size(); ++i) {
             const MNode &nd = wave[i];
             if (nd.slot != kNoSlot) {
-                count_src[i] = {0, t_items.size()};
+                count_src[i] = {0, n_ti};
                 if (nd.tail.empty()) continue;
-                for (uint32_t e : nd.tail) t_items.push_back(prow(nd, e));
-                t_ptr.push_back(t_items.size());
+                n_ti += nd.tail.size();
+                t_ptr.push_back(n_ti);
                 t_slot.push_back(nd.slot);
             } else {
                 count_src[i] = {1, qs.size()};
@@ -647,6 +673,16 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 }
             }
         }
+        t_items.resize(n_ti);
+        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                const MNode &nd = wave[i];
+                if (nd.slot == kNoSlot || nd.tail.empty()) continue;
+                const uint32_t off = (use_proj_ && nd.proj != kNoProj) ? (uint32_t)root_slot_[nd.proj] * d : 0u;
+                uint32_t *dst = t_items.data() + count_src[i].second;
+                for (size_t j = 0; j < nd.tail.size(); ++j) dst[j] = nd.tail[j] + off;
+            }
+        });
         timed(0, [&] {
             run_tail_counts(t_ptr, t_items, t_slot, counts);
             run_queries(qs, vrows_, vstride_, vwords_, vd_, QUERY_COUNT, counts_q);
@@ -694,20 +730,37 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 }
             }
         });
-        qpool.clear();
-        qfhut.clear();
         const bool slot_pools = use_spool_ && !wave_global;
         uint64_t spool_max = 0;   // candidates in the largest slot pool the wave reads
+        uint64_t n_pi = 0, n_fi = 0;
+        qpool.ptr.resize(wave.size() + 1);
+        qpool.ptr[0] = 0;
+        qpool.slot.assign(wave.size(), kNoSlot);
+        qfhut.ptr.assign(1, 0);
+        qfhut.slot.clear();
         for (size_t i = 0; i < wave.size(); ++i) {
             Work &wk = work[i];
-            wk.pool_q = qpool.size();
-            qpool.add(wk.pq.data(), wk.pq.size(), kNoSlot);
+            wk.pool_q = i;
+            n_pi += wk.pq.size();
+            qpool.ptr[i + 1] = n_pi;
             if (wk.kind == 1) {
-                wk.fhut_q = qfhut.size();
-                qfhut.add(wk.fq.data(), wk.fq.size(), wave[i].slot);
+                wk.fhut_q = qfhut.slot.size();
+                wk.fi0 = n_fi;
+                n_fi += wk.fq.size();
+                qfhut.ptr.push_back(n_fi);
+                qfhut.slot.push_back(wave[i].slot);
             }
             if (slot_pools) spool_max = std::max(spool_max, spool_n_[root_slot_[wave[i].proj]]);
         }
+        qpool.items.resize(n_pi);
+        qfhut.items.resize(n_fi);
+        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                const Work &wk = work[i];
+                std::copy(wk.pq.begin(), wk.pq.end(), qpool.items.begin() + qpool.ptr[i]);
+                if (wk.kind == 1) std::copy(wk.fq.begin(), wk.fq.end(), qfhut.items.begin() + wk.fi0);
+            }
+        });
         add_since(6, t_exp);
         if (slot_pools && spool_max > 0) {
             const uint64_t pw = ((spool_max + 63) / 64 + 1) & ~1ull;
@@ -762,6 +815,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             csup_.resize(c0 + n_emit);
             cnode_.resize(c0 + n_emit);
             hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+                std::vector<uint32_t> freq(d, 0);   // this chunk's candidates per item
                 for (uint64_t i = lo; i < hi; ++i) {
                     const Work &wk = work[i];
                     if (!wk.emit) continue;
@@ -770,15 +824,17 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                     if (wk.kind == 2)
                         for (auto &pr : wk.f) *e++ = pr.second;
                     std::sort(dst, e);
+                    for (const uint32_t *x = dst; x < e; ++x) ++freq[*x];
                     cptr_[c0 + 1 + wk.e0] = (uint64_t)(e - citems_.data());
                     csup_[c0 + wk.e0] = wk.kind == 2 ? fhut_cnt[wk.fhut_q] : wave[i].sup;
                     cnode_[c0 + wk.e0] = wave[i].id;
                 }
+                for (uint32_t x = 0; x < d; ++x)
+                    if (freq[x]) __atomic_fetch_add(&cand_freq_[x], (uint64_t)freq[x], __ATOMIC_RELAXED);
             });
             ctime_.resize(c0 + n_emit, elapsed());
             cexpanded_.resize(c0 + n_emit, nodes_);
             ccheck_.resize(c0 + n_emit, pool_n_);
-            for (uint64_t k = it0; k < citems_.size(); ++k) ++cand_freq_[citems_[k]];
         }
         // features of the expanding nodes' extensions (F in ascending support; the
         // position feature is that rank)
@@ -801,13 +857,11 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         t_exp = Clock::now();
         // children in the order's sequence: the p-th extension's tail is the
         // extensions after it, and the first is searched first
-        kids.clear();
-        kids.resize(n_ext);
+        // (kids keeps its elements from wave to wave: they were moved to the stack, so
+        // each is reset below; the spare vectors are handed out by position)
+        if (kids.size() < n_ext) kids.resize(n_ext);
         kid_src.resize(n_ext);
-        for (MNode &c : kids) {
-            c.head = take_spare();
-            c.tail = take_spare();
-        }
+        const uint64_t n_spare = std::min<uint64_t>(spare_.size() / 2, n_ext), sp0 = spare_.size() - 2 * n_spare;
         const uint64_t id0 = parent_.size(), tr0 = tnode_.size();
         parent_.resize(id0 + n_ext);
         if (p_.record_trace) {
@@ -836,6 +890,11 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                     const uint32_t j = rank[p];
                     const uint64_t k = wk.kid0 + p;
                     MNode &c = kids[k];
+                    if (k < n_spare) {
+                        c.head = std::move(spare_[sp0 + 2 * k]);
+                        c.tail = std::move(spare_[sp0 + 2 * k + 1]);
+                    }
+                    c.slot = kNoSlot;
                     c.head.assign(wk.head.begin(), wk.head.end());
                     c.head.push_back(wk.f[j].second);
                     c.sup = wk.f[j].first;
@@ -852,11 +911,12 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
                 }
             }
         });
+        spare_.resize(sp0);
         add_since(6, t_exp);
         // child masks for the children searched next: mask(child) = mask(parent) & row(e)
         qchild.clear();
         child_slot.clear();
-        for (size_t k = 0; k < kids.size(); ++k) {
+        for (size_t k = 0; k < n_ext; ++k) {
             MNode &c = kids[k];
             // leaves need no mask; a root child gets its mask once its projection is resident
             if (c.tail.empty() || (use_proj_ && (c.proj == kNoProj || root_slot_[c.proj] < 0))) continue;
@@ -883,13 +943,18 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         // the stack is LIFO: push in reverse so that the wave's first node's first
         // child is popped first
         t_exp = Clock::now();
-        for (size_t i = wave.size(); i-- > 0;) {
-            Work &wk = work[i];
-            if (wk.kind != 3) continue;
-            for (size_t j = wk.kid0 + wk.nkids; j-- > wk.kid0;) {
-                if (use_proj_ && kids[j].proj != kNoProj) ++live_[kids[j].proj];
-                stack.push_back(std::move(kids[j]));
-            }
+        // (the expanding nodes' kid ranges ascend in wave order, so this is the kid
+        // list reversed)
+        {
+            const size_t sb = stack.size();
+            stack.resize(sb + n_ext);
+            hp_.run(n_ext, 4096, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t k = lo; k < hi; ++k) {
+                    if (use_proj_ && kids[k].proj != kNoProj)
+                        __atomic_fetch_add(&live_[kids[k].proj], 1u, __ATOMIC_RELAXED);
+                    stack[sb + n_ext - 1 - k] = std::move(kids[k]);
+                }
+            });
         }
         // parents' masks are no longer needed once the child-mask kernel ran (stream order)
         for (MNode &nd : wave) {

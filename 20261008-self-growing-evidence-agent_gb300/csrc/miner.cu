@@ -534,15 +534,20 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
     const uint64_t slot_bytes = slot_words_ * 8;
     const uint64_t budget = h_->hbm_budget / 4;
     uint64_t max_slots = std::min<uint64_t>(1u << 20, budget / std::max<uint64_t>(slot_bytes, 1));
-    max_slots = std::min<uint64_t>(max_slots, std::max<uint64_t>(4096, (uint64_t)freq.size() * 64));
+    // up to 256 masks per frequent item: the stack's pending children keep their
+    // masks (at 64 per item, 35k children of the 2% anytime-2m search had to
+    // rebuild theirs from head rows later)
+    max_slots = std::min<uint64_t>(max_slots, std::max<uint64_t>(4096, (uint64_t)freq.size() * 256));
     if (max_slots < 64) max_slots = 64;
     arena_.reserve(max_slots * slot_bytes, st);
     free_slots_.resize(max_slots);
     for (uint64_t i = 0; i < max_slots; ++i) free_slots_[i] = (uint32_t)(max_slots - 1 - i);
     pool_reserve(65536);
 
-    const uint64_t qmax = 1u << 17;                                // queries per wave
-    const uint64_t nmax = h_->wave_nodes ? h_->wave_nodes : 8192;  // nodes per wave
+    // nodes per wave, and tail entries per wave (16 per node); wider waves mean
+    // fewer round trips and the same tree (node counts equal at 32 ... 32,768)
+    const uint64_t nmax = h_->wave_nodes ? h_->wave_nodes : 32768;
+    const uint64_t qmax = std::max<uint64_t>(1u << 17, nmax * 16);
     std::vector<MNode> stack;
     if (!freq.empty()) {
         MNode root;

@@ -38,6 +38,12 @@ from .mlp import IN_DIM, Trainer
 
 FAMILY = dict(n_sensors=80, n_bins=8, n_regimes=32, alpha_bin=0.2)
 COVERAGE = (0.5, 0.9, 0.95)
+# Orders are compared at 8,192 search nodes per wave, every order alike: the
+# engine's default wave (32,768) finishes the smaller 3% streams in a handful
+# of waves, and a wave's candidates all come out at its end, so the time to a
+# coverage level would measure the wave grid rather than the order.  Node
+# counts do not depend on the wave size.
+EVAL_WAVE_NODES = 8192
 
 
 def stream_rows(seed, n_txn):
@@ -109,7 +115,7 @@ def evaluate_committed(weights_path, n_seeds=3, n_txn=2_000_000, floor=0.03, fir
     """Held-out streams of the anytime-2m family with committed scorer weights:
     coverage times and nodes of the learned, canonical and plain orders, final
     sets compared."""
-    with Engine() as eng:
+    with Engine(wave_nodes=EVAL_WAVE_NODES) as eng:
         load_weights(eng, weights_path)
         rows = evaluate(eng, range(first_seed, first_seed + n_seeds), n_txn, floor)
     return {"n_txn": n_txn, "floor": floor, "summary": summarize(rows), "runs": rows}
@@ -127,7 +133,7 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
-    eng = Engine()
+    eng = Engine(wave_nodes=EVAL_WAVE_NODES)
     t0 = time.time()
     X, Y, tstats = collect_traces(eng, range(1000, 1000 + a.train_seeds), a.n_txn, a.floor)
     t_trace = time.time() - t0

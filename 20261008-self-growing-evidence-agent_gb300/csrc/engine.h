@@ -138,13 +138,13 @@ struct WindowWorkspace {
 // that repeated mining (anytime stages, window services) allocates nothing
 // once warm.
 struct MinerWorkspace {
-    DevBuf arena, pool, q_out, score, cooc, t_out, pdb, pofs, spool;
+    DevBuf arena, pool, q_out, score, cooc, t_out, pdb, pofs, pmask, spool;
     HostBuf hq_out, hscore, ht_out;
     Staged q_ptr, q_items, q_slot, c_ptr, c_items, c_ps, c_cs, p_ptr, p_items, feat, w0, t_ptr, t_items, t_slot,
         p_items_list, s_ptr, s_items, s_cols;
     void release() {
         arena.release(); pool.release(); q_out.release(); score.release(); cooc.release(); t_out.release();
-        pdb.release(); pofs.release(); spool.release();
+        pdb.release(); pofs.release(); pmask.release(); spool.release();
         hq_out.release(); hscore.release(); ht_out.release();
         for (Staged *s : {&q_ptr, &q_items, &q_slot, &c_ptr, &c_items, &c_ps, &c_cs, &p_ptr, &p_items, &feat, &w0,
                           &t_ptr, &t_items, &t_slot, &p_items_list, &s_ptr, &s_items, &s_cols})

@@ -117,9 +117,10 @@ void launch_wait_probe(uint32_t *err, cudaStream_t st);
 // Projected database of one item (the miner's root subtrees): out row e (for
 // every e in items, out_words <= out_stride words, all d rows zeroed first)
 // holds the bits of row e at the transactions of row root_row, packed in order.
+// Scratch: ofs n_words x 4 B, masks 6 x n_words x 8 B.
 void launch_projection(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t root_row,
-                       const uint32_t *items, uint32_t n_items, uint32_t *ofs, uint64_t *out, uint64_t out_stride,
-                       uint64_t out_words, uint32_t d, cudaStream_t st, int n_sm);
+                       const uint32_t *items, uint32_t n_items, uint32_t *ofs, uint64_t *masks, uint64_t *out,
+                       uint64_t out_stride, uint64_t out_words, uint32_t d, cudaStream_t st, int n_sm);
 
 // Miner helpers.
 // mask(child c) = (parent_slot[c] != kNoSlot ? arena[parent_slot[c]] : ones) & AND rows(items[ptr[c]..ptr[c+1]))

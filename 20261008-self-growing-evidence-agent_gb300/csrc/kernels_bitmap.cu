@@ -972,28 +972,51 @@ __global__ void __launch_bounds__(1024) row_prefix_kernel(const uint64_t *__rest
     }
 }
 
+// The move masks of the compress (generalized extract) of each root word m,
+// after H. S. Warren, Hacker's Delight, 2nd ed., section 7-4: six steps, step i
+// shifting the bits in masks[i] right by 2^i, pack the bits of x under m to the
+// low end in order.  The masks depend on m alone, so they are computed once per
+// root and used for every projected row (masks[i * n_words + w]).
+__global__ void root_masks_kernel(const uint64_t *__restrict__ root, uint64_t n_words, uint64_t *__restrict__ masks) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t m = root[w];
+        uint64_t mk = ~m << 1;   // ones at positions whose lower neighbour is a zero of m
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            uint64_t mp = mk ^ (mk << 1);   // parallel suffix (prefix xor towards the high end)
+            mp ^= mp << 2;
+            mp ^= mp << 4;
+            mp ^= mp << 8;
+            mp ^= mp << 16;
+            mp ^= mp << 32;
+            const uint64_t mv = mp & m;     // bits that move by 2^i in this step
+            m = (m ^ mv) | (mv >> (1 << i));
+            mk &= ~mp;
+            masks[(uint64_t)i * n_words + w] = mv;
+        }
+    }
+}
+
 // Row items[blockIdx.y] of the projection: the bits of that bitmap row at the set
 // positions of `root`, packed in transaction order (out rows zeroed beforehand).
 __global__ void project_rows_kernel(const uint64_t *__restrict__ rows, uint64_t stride, uint64_t n_words,
                                     const uint64_t *__restrict__ root, const uint32_t *__restrict__ ofs,
-                                    const uint32_t *__restrict__ items, unsigned long long *__restrict__ out,
-                                    uint64_t out_stride) {
+                                    const uint64_t *__restrict__ masks, const uint32_t *__restrict__ items,
+                                    unsigned long long *__restrict__ out, uint64_t out_stride) {
     const uint32_t e = items[blockIdx.y];
     const uint64_t *src = rows + (uint64_t)e * stride;
     unsigned long long *dst = out + (uint64_t)e * out_stride;
     for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t m = root[w];
+        const uint64_t m = root[w];
         if (!m) continue;
-        const uint64_t v = src[w];
-        uint64_t p = 0;
-        uint32_t nb = 0;
-        while (m) {   // bit extraction under the mask, lowest transaction first
-            const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
-            p |= ((v >> b) & 1ull) << nb;
-            ++nb;
-            m &= m - 1;
-        }
+        uint64_t p = src[w] & m;
         if (!p) continue;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const uint64_t t = p & masks[(uint64_t)i * n_words + w];
+            p = (p ^ t) | (t >> (1 << i));
+        }
+        const uint32_t nb = popc64(m);
         const uint32_t o = ofs[w], sh = o & 63;
         atomicOr(dst + (o >> 6), (unsigned long long)(p << sh));
         if (sh && sh + nb > 64) atomicOr(dst + (o >> 6) + 1, (unsigned long long)(p >> (64 - sh)));
@@ -1001,16 +1024,19 @@ __global__ void project_rows_kernel(const uint64_t *__restrict__ rows, uint64_t 
 }
 
 void launch_projection(const uint64_t *rows, uint64_t stride, uint64_t n_words, uint32_t root_row,
-                       const uint32_t *items, uint32_t n_items, uint32_t *ofs, uint64_t *out, uint64_t out_stride,
-                       uint64_t out_words, uint32_t d, cudaStream_t st, int n_sm) {
+                       const uint32_t *items, uint32_t n_items, uint32_t *ofs, uint64_t *masks, uint64_t *out,
+                       uint64_t out_stride, uint64_t out_words, uint32_t d, cudaStream_t st, int n_sm) {
     SG_CUDA_TRY(cudaMemset2DAsync(out, out_stride * 8, 0, out_words * 8, d, st));
     if (n_items == 0 || n_words == 0) return;
     const uint64_t *root = rows + (uint64_t)root_row * stride;
     row_prefix_kernel<<<1, 1024, 0, st>>>(root, n_words, ofs);
     SG_CUDA_TRY(cudaGetLastError());
+    root_masks_kernel<<<(unsigned)std::min<uint64_t>((n_words + 255) / 256, (uint64_t)n_sm * 8), 256, 0, st>>>(
+        root, n_words, masks);
+    SG_CUDA_TRY(cudaGetLastError());
     const unsigned bx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n_words + 255) / 256,
                                                                             (uint64_t)n_sm * 16 / std::max(1u, n_items) + 1));
-    project_rows_kernel<<<dim3(bx, n_items), 256, 0, st>>>(rows, stride, n_words, root, ofs, items,
+    project_rows_kernel<<<dim3(bx, n_items), 256, 0, st>>>(rows, stride, n_words, root, ofs, masks, items,
                                                            reinterpret_cast<unsigned long long *>(out), out_stride);
     SG_CUDA_TRY(cudaGetLastError());
 }

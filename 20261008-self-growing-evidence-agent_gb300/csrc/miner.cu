@@ -464,9 +464,10 @@ bool Miner::make_resident(const MNode &nd) {
     // whole rows are cleared: a wave reads up to its widest projection, so every
     // row must be zero past its own projection's words
     launch_projection(ds_.bitmaps.as<uint64_t>(), ds_.stride, ds_.n_words, r, ditems, (uint32_t)items.size(),
-                      w_.pofs.as<uint32_t>(), w_.pdb.as<uint64_t>() + (uint64_t)slot * ds_.d * proj_stride_,
+                      w_.pofs.as<uint32_t>(), w_.pmask.as<uint64_t>(),
+                      w_.pdb.as<uint64_t>() + (uint64_t)slot * ds_.d * proj_stride_,
                       proj_stride_, proj_stride_, ds_.d, st, h_->n_sm);
-    launches_ += 2;
+    launches_ += 3;
     ++projections_;
     if (use_spool_) {
         // the pool projected on r's pool row: every candidate so far (all are in the
@@ -474,10 +475,12 @@ bool Miner::make_resident(const MNode &nd) {
         spool_reserve(cand_freq_[r]);
         const uint64_t pw = pool_n_ ? ((pool_n_ + 63) / 64 + 1) & ~1ull : 0;
         w_.pofs.reserve(std::max<uint64_t>(pw, 1) * 4, st);
+        w_.pmask.reserve(std::max<uint64_t>(pw, 1) * 6 * 8, st);
         launch_projection(pool_.as<uint64_t>(), pool_words_, pw, r, ditems, (uint32_t)items.size(),
-                          w_.pofs.as<uint32_t>(), w_.spool.as<uint64_t>() + (uint64_t)slot * ds_.d * spool_words_,
+                          w_.pofs.as<uint32_t>(), w_.pmask.as<uint64_t>(),
+                          w_.spool.as<uint64_t>() + (uint64_t)slot * ds_.d * spool_words_,
                           spool_words_, spool_words_, ds_.d, st, h_->n_sm);
-        launches_ += 2;
+        launches_ += 3;
         spool_n_[slot] = cand_freq_[r];
     }
     slot_root_[slot] = r;
@@ -522,6 +525,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             1, std::min<uint64_t>(kProjSlots, (h_->hbm_budget / 8) / std::max<uint64_t>(slot_bytes, 1)));
         w_.pdb.reserve((size_t)n_proj_slots_ * slot_bytes, st);
         w_.pofs.reserve((size_t)std::max<uint64_t>(ds_.n_words, 1) * 4, st);
+        w_.pmask.reserve((size_t)std::max<uint64_t>(ds_.n_words, 1) * 6 * 8, st);
         slot_root_.assign(n_proj_slots_, kNoProj);
         root_slot_.assign(d, -1);
         live_.assign(d, 0);

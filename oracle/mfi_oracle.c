@@ -22,6 +22,12 @@
  *                       HUT/FHUT look-ahead and tidset projection, used where
  *                       mine_mfi's 200k-node cap makes the reference miner
  *                       unusable; it is checked against orc_mine_dfs.
+ *   orc_mine_fast_order the same search with the extensions of every node in
+ *                       ascending support (order 0, orc_mine_fast) or in the
+ *                       reference's global descending-support order
+ *                       (order 1: kernel_bitmap.cu:276-283,
+ *                       code/pipeline/exp_e6_cpuvec.py:65-69); the set is
+ *                       the same, the tree is not.
  *
  * Layout: bitmaps are uint64 [d][W] row-major; bit (t & 63) of word (t >> 6)
  * of row e is set when transaction t holds dense item e.
@@ -425,6 +431,10 @@ done:
 typedef struct {
     uint32_t d, words;     /* item count, u64 words per item bitset */
     uint32_t thr;
+    int order;             /* 0: ascending support in the node's context; 1: one global order,
+                              descending item support, ties ascending id (kernel_bitmap.cu:276-283,
+                              exp_e6_cpuvec.py:65-69) */
+    uint32_t *gsup;        /* item supports (order 1) */
     rbuf pool;             /* candidates (sorted items) */
     uint64_t *pool_bits;   /* words per candidate */
     uint64_t pool_cap;
@@ -500,6 +510,27 @@ static int cmp_isup(const void *a, const void *b) {
     return (x->item > y->item) - (x->item < y->item);
 }
 
+/* x before y in the search order of the extensions */
+static int ext_before(const fast_ctx *c, const isup *x, const isup *y) {
+    if (c->order == 1) {
+        const uint32_t p = c->gsup[x->item], q = c->gsup[y->item];
+        if (p != q) return p > q;
+        return x->item < y->item;
+    }
+    if (x->sup != y->sup) return x->sup < y->sup;
+    return x->item < y->item;
+}
+
+/* stable insertion sort of the extensions (F is at most d long) */
+static void sort_ext(const fast_ctx *c, isup *g, uint32_t n) {
+    for (uint32_t i = 1; i < n; i++) {
+        isup v = g[i];
+        uint32_t j = i;
+        while (j > 0 && ext_before(c, &v, &g[j - 1])) { g[j] = g[j - 1]; j--; }
+        g[j] = v;
+    }
+}
+
 /* tail bitmaps: tb[i] is the (possibly projected) bitmap of tail item i, nw words;
  * head bitmap hb is over the same transaction space. */
 static int fast_rec(fast_ctx *c, uint32_t depth, uint32_t *head, uint32_t hk, uint64_t *hbits,
@@ -525,7 +556,8 @@ static int fast_rec(fast_ctx *c, uint32_t depth, uint32_t *head, uint32_t hk, ui
         if (h2 > 0 && !covered(c, depth, hbits)) rc = pool_add(c, head, h2, hsup, depth);
         goto out;
     }
-    /* order F by ascending support, ties by ascending item id */
+    /* order F: ascending support, ties by ascending item id (order 0), or the
+     * global descending-support order (order 1) */
     for (uint32_t i = 0; i < nf; i++) { fidx[i] = f[i].item; f[i].item = tail[fidx[i]]; }
     {
         /* keep the tail-index association through the sort */
@@ -533,7 +565,8 @@ static int fast_rec(fast_ctx *c, uint32_t depth, uint32_t *head, uint32_t hk, ui
         uint32_t *map = (uint32_t *)malloc((c->d + 1) * sizeof(uint32_t));
         if (!g || !map) { free(g); free(map); rc = -1; goto out; }
         for (uint32_t i = 0; i < nf; i++) { g[i] = f[i]; map[f[i].item] = fidx[i]; }
-        qsort(g, nf, sizeof(isup), cmp_isup);
+        if (c->order == 0) qsort(g, nf, sizeof(isup), cmp_isup);
+        else sort_ext(c, g, nf);
         for (uint32_t i = 0; i < nf; i++) { f[i] = g[i]; fidx[i] = map[g[i].item]; }
         free(g); free(map);
     }
@@ -626,15 +659,25 @@ out:
 
 /* Exact MFI set at absolute threshold thr (every MFI once, with its support).
  * Returns 0, 1 on node-cap overflow, -1 on allocation failure. */
-int orc_mine_fast(const uint64_t *bm, uint32_t d, uint64_t W, uint64_t n_txn, uint32_t thr,
-                  uint64_t node_cap, orc_mfis *out) {
+int orc_mine_fast_order(const uint64_t *bm, uint32_t d, uint64_t W, uint64_t n_txn, uint32_t thr,
+                        uint64_t node_cap, int order, orc_mfis *out) {
     memset(out, 0, sizeof(*out));
     if (thr < 1) thr = 1;
+    if (order < 0 || order > 1) return -1;
     fast_ctx c;
     memset(&c, 0, sizeof(c));
     c.d = d; c.words = (d + 63) / 64; if (!c.words) c.words = 1;
-    c.thr = thr; c.cap = node_cap;
+    c.thr = thr; c.cap = node_cap; c.order = order;
     int rc = 0;
+    if (order == 1) {
+        c.gsup = (uint32_t *)calloc(d ? d : 1, sizeof(uint32_t));
+        if (!c.gsup) return -1;
+        for (uint32_t e = 0; e < d; e++) {
+            uint32_t s = 0;
+            for (uint64_t w = 0; w < W; w++) s += POPC64(bm[(size_t)e * W + w]);
+            c.gsup[e] = s;
+        }
+    }
     if (rb_init(&c.pool)) return -1;
     c.lmfi = (uint32_t **)calloc(d + 2, sizeof(uint32_t *));
     c.lmfi_n = (uint64_t *)calloc(d + 2, sizeof(uint64_t));
@@ -657,5 +700,11 @@ done:
     if (c.lmfi) for (uint32_t i = 0; i < d + 2; i++) free(c.lmfi[i]);
     free(c.lmfi); free(c.lmfi_n); free(c.lmfi_cap);
     free(head); free(hbits); free(all); free(tail); free(tb);
+    free(c.gsup);
     return rc;
+}
+
+int orc_mine_fast(const uint64_t *bm, uint32_t d, uint64_t W, uint64_t n_txn, uint32_t thr,
+                  uint64_t node_cap, orc_mfis *out) {
+    return orc_mine_fast_order(bm, d, W, n_txn, thr, node_cap, 0, out);
 }

@@ -53,6 +53,8 @@ def lib():
         L.orc_cooccurrence.argtypes = [u64p, C.c_uint32, C.c_uint64, u32p, C.c_int]
         L.orc_mine_dfs.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_mine_fast.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
+        L.orc_mine_fast_order.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int,
+                                          C.POINTER(_Mfis)]
         L.orc_mine_engine.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint32, u32p, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_free.argtypes = [C.POINTER(_Mfis)]
         L.orc_online_bins.argtypes = [C.POINTER(C.c_double), C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
@@ -61,7 +63,7 @@ def lib():
         L.orc_planted_kat.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, u32p, u32p, u32p,
                                       C.POINTER(C.c_double)]
         L.orc_planted_kat.restype = C.c_int
-        for f in ("orc_mine_dfs", "orc_mine_fast", "orc_mine_engine"):
+        for f in ("orc_mine_dfs", "orc_mine_fast", "orc_mine_fast_order", "orc_mine_engine"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -150,12 +152,16 @@ def mine_mfi(bm, n_txn, min_sup=0.05, min_count=None, node_cap=0):
     return _collect(m), nodes
 
 
-def mine_fast(bm, n_txn, thr, node_cap=0):
-    """Pruned exact MFI miner (PEP/HUT/FHUT, projection): [(items, support)], nodes."""
+def mine_fast(bm, n_txn, thr, node_cap=0, order="support"):
+    """Pruned exact MFI miner (PEP/HUT/FHUT, projection): [(items, support)], nodes.
+    ``order``: "support" (each node's extensions in ascending support) or
+    "support_desc" (the reference's global descending-support order); the set
+    is the same, the number of nodes is not."""
     bm = np.ascontiguousarray(bm, dtype=np.uint64)
     m = _Mfis()
-    rc = lib().orc_mine_fast(_p(bm, C.c_uint64), bm.shape[0], bm.shape[1], n_txn, max(1, int(thr)),
-                             node_cap, C.byref(m))
+    code = {"support": 0, "support_desc": 1}[order]
+    rc = lib().orc_mine_fast_order(_p(bm, C.c_uint64), bm.shape[0], bm.shape[1], n_txn, max(1, int(thr)),
+                                   node_cap, code, C.byref(m))
     nodes = int(m.nodes)
     if rc == 1:
         lib().orc_free(C.byref(m))

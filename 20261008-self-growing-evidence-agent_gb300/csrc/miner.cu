@@ -46,6 +46,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <thread>
 
@@ -194,8 +195,10 @@ class Miner {
     DevBuf &q_out_, &score_;
     HostBuf &hq_out_, &hscore_;
     uint64_t nodes_ = 0, waves_ = 0, launches_ = 0;
-    // per-node bookkeeping of a wave (PEP, extension order, candidates, children)
-    HostPool hp_{std::min(16u, std::max(1u, std::thread::hardware_concurrency()))};
+    // per-node bookkeeping of a wave (PEP, extension order, candidates, children):
+    // host threads on large datasets; one (the caller) on small ones, whose waves
+    // are small and whose callers may run many miners at once (one per window)
+    std::unique_ptr<HostPool> hp_;
     // vectors of finished nodes, reused for new children (no allocation per node once warm)
     std::vector<std::vector<uint32_t>> spare_;
     std::vector<uint64_t> cand_freq_;   // candidates holding each dense item (pool row density)
@@ -348,7 +351,7 @@ void Miner::flush_pool(uint64_t from) {
     // (a slot's columns are taken from its counter, in any order: a slot pool is a set)
     const uint64_t nn = n - from;
     sp_cnt_.assign(nn + 1, 0);
-    hp_.run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
+    hp_->run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
         for (uint64_t i = lo; i < hi; ++i) {
             uint64_t k = 0;
             for (uint64_t j = cptr_[from + i]; j < cptr_[from + i + 1]; ++j) k += root_slot_[citems_[j]] >= 0;
@@ -367,7 +370,7 @@ void Miner::flush_pool(uint64_t from) {
     sp_ptr_.resize(n_ent + 1);
     sp_cols_.resize(n_ent);
     sp_ptr_[n_ent] = sp_io_[nn];
-    hp_.run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
+    hp_->run(nn, 2048, [&](uint64_t lo, uint64_t hi) {
         for (uint64_t i = lo; i < hi; ++i) {
             const uint64_t a = cptr_[from + i], b = cptr_[from + i + 1];
             uint64_t e = sp_cnt_[i], at = sp_io_[i];
@@ -512,6 +515,8 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         if (ds_.sup[e] >= thr_) freq.push_back(e);
     std::stable_sort(freq.begin(), freq.end(), [&](uint32_t a, uint32_t b) { return ds_.sup[a] < ds_.sup[b]; });
 
+    hp_ = std::make_unique<HostPool>(
+        ds_.n_words >= 2048 ? std::min(16u, std::max(1u, std::thread::hardware_concurrency())) : 1u);
     // projected root subtrees on large datasets (SGFIM_F_NO_PROJECTION / SGFIM_F_PROJECT override)
     view_global();
     use_proj_ = (h_->flags & SGFIM_F_PROJECT) ||
@@ -594,7 +599,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         {
             const size_t s0 = spare_.size();
             spare_.resize(s0 + 2 * wave.size());
-            hp_.run(wave.size(), 2048, [&](uint64_t lo, uint64_t hi) {
+            hp_->run(wave.size(), 2048, [&](uint64_t lo, uint64_t hi) {
                 for (uint64_t i = lo; i < hi; ++i) {
                     wave[i].head.clear();
                     wave[i].tail.clear();
@@ -683,7 +688,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             }
         }
         t_items.resize(n_ti);
-        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+        hp_->run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
             for (uint64_t i = lo; i < hi; ++i) {
                 const MNode &nd = wave[i];
                 if (nd.slot == kNoSlot || nd.tail.empty()) continue;
@@ -700,7 +705,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         // the host pool, then the query lists concatenated in wave order
         auto t_exp = Clock::now();
         if (work.size() < wave.size()) work.resize(wave.size());
-        hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+        hp_->run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
             for (uint64_t i = lo; i < hi; ++i) {
                 const MNode &nd = wave[i];
                 Work &wk = work[i];
@@ -763,7 +768,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         }
         qpool.items.resize(n_pi);
         qfhut.items.resize(n_fi);
-        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+        hp_->run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
             for (uint64_t i = lo; i < hi; ++i) {
                 const Work &wk = work[i];
                 std::copy(wk.pq.begin(), wk.pq.end(), qpool.items.begin() + qpool.ptr[i]);
@@ -786,7 +791,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         // ---- phase C: leaf and FHUT candidates, HUT, expanding nodes
         t_exp = Clock::now();
         const uint64_t pool_before = csup_.size();
-        hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+        hp_->run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
             for (uint64_t i = lo; i < hi; ++i) {
                 Work &wk = work[i];
                 if (wk.kind == 0) {
@@ -823,7 +828,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             cptr_.resize(c0 + 1 + n_emit);
             csup_.resize(c0 + n_emit);
             cnode_.resize(c0 + n_emit);
-            hp_.run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
+            hp_->run(wave.size(), 1024, [&](uint64_t lo, uint64_t hi) {
                 std::vector<uint32_t> freq(d, 0);   // this chunk's candidates per item
                 for (uint64_t i = lo; i < hi; ++i) {
                     const Work &wk = work[i];
@@ -849,7 +854,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         // position feature is that rank)
         if (need_feat_) {
             wfeat.resize(n_ext * kDim);
-            hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+            hp_->run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
                 for (uint64_t i = lo; i < hi; ++i) {
                     const Work &wk = work[i];
                     if (wk.kind != 3) continue;
@@ -877,7 +882,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
             tfeat_.resize((tr0 + n_ext) * kDim);
             tnode_.resize(tr0 + n_ext);
         }
-        hp_.run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
+        hp_->run(wave.size(), 256, [&](uint64_t lo, uint64_t hi) {
             std::vector<uint32_t> rank;
             for (uint64_t i = lo; i < hi; ++i) {
                 const MNode &nd = wave[i];
@@ -957,7 +962,7 @@ int Miner::run(const double *ckpts, uint32_t n_ckpt, sgfim_ckpt_cb cb, void *use
         {
             const size_t sb = stack.size();
             stack.resize(sb + n_ext);
-            hp_.run(n_ext, 4096, [&](uint64_t lo, uint64_t hi) {
+            hp_->run(n_ext, 4096, [&](uint64_t lo, uint64_t hi) {
                 for (uint64_t k = lo; k < hi; ++k) {
                     if (use_proj_ && kids[k].proj != kNoProj)
                         __atomic_fetch_add(&live_[kids[k].proj], 1u, __ATOMIC_RELAXED);

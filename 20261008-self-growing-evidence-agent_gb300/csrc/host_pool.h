@@ -5,7 +5,9 @@
 // counter by the caller and the pool's threads, and returns when every chunk
 // is done.  The threads start on first use.  Between calls they poll for the
 // next job for a short while (a wave issues several jobs within a
-// millisecond or two), then sleep on a condition variable.
+// millisecond or two), then sleep on a condition variable.  One owner thread
+// issues the jobs, one at a time: run() is not reentrant (fn must not call it)
+// and a pool is not shared between threads (each miner owns its own).
 #pragma once
 
 #include <stdint.h>

@@ -26,8 +26,11 @@
  *                       ascending support (order 0, orc_mine_fast) or in the
  *                       reference's global descending-support order
  *                       (order 1: kernel_bitmap.cu:276-283,
- *                       code/pipeline/exp_e6_cpuvec.py:65-69); the set is
- *                       the same, the tree is not.
+ *                       code/pipeline/exp_e6_cpuvec.py:65-69), or in one
+ *                       global order of a caller's per-item key (order 2,
+ *                       no reference counterpart: a bound on what any
+ *                       static order achieves); the set is the same, the
+ *                       tree is not.
  *
  * Layout: bitmaps are uint64 [d][W] row-major; bit (t & 63) of word (t >> 6)
  * of row e is set when transaction t holds dense item e.
@@ -433,8 +436,10 @@ typedef struct {
     uint32_t thr;
     int order;             /* 0: ascending support in the node's context; 1: one global order,
                               descending item support, ties ascending id (kernel_bitmap.cu:276-283,
-                              exp_e6_cpuvec.py:65-69) */
+                              exp_e6_cpuvec.py:65-69); 2: one global order, ascending caller key,
+                              ties ascending id */
     uint32_t *gsup;        /* item supports (order 1) */
+    const double *key;     /* per-item key (order 2) */
     rbuf pool;             /* candidates (sorted items) */
     uint64_t *pool_bits;   /* words per candidate */
     uint64_t pool_cap;
@@ -512,6 +517,11 @@ static int cmp_isup(const void *a, const void *b) {
 
 /* x before y in the search order of the extensions */
 static int ext_before(const fast_ctx *c, const isup *x, const isup *y) {
+    if (c->order == 2) {
+        const double p = c->key[x->item], q = c->key[y->item];
+        if (p != q) return p < q;
+        return x->item < y->item;
+    }
     if (c->order == 1) {
         const uint32_t p = c->gsup[x->item], q = c->gsup[y->item];
         if (p != q) return p > q;
@@ -660,14 +670,14 @@ out:
 /* Exact MFI set at absolute threshold thr (every MFI once, with its support).
  * Returns 0, 1 on node-cap overflow, -1 on allocation failure. */
 int orc_mine_fast_order(const uint64_t *bm, uint32_t d, uint64_t W, uint64_t n_txn, uint32_t thr,
-                        uint64_t node_cap, int order, orc_mfis *out) {
+                        uint64_t node_cap, int order, const double *key, orc_mfis *out) {
     memset(out, 0, sizeof(*out));
     if (thr < 1) thr = 1;
-    if (order < 0 || order > 1) return -1;
+    if (order < 0 || order > 2 || (order == 2 && !key)) return -1;
     fast_ctx c;
     memset(&c, 0, sizeof(c));
     c.d = d; c.words = (d + 63) / 64; if (!c.words) c.words = 1;
-    c.thr = thr; c.cap = node_cap; c.order = order;
+    c.thr = thr; c.cap = node_cap; c.order = order; c.key = key;
     int rc = 0;
     if (order == 1) {
         c.gsup = (uint32_t *)calloc(d ? d : 1, sizeof(uint32_t));
@@ -706,5 +716,5 @@ done:
 
 int orc_mine_fast(const uint64_t *bm, uint32_t d, uint64_t W, uint64_t n_txn, uint32_t thr,
                   uint64_t node_cap, orc_mfis *out) {
-    return orc_mine_fast_order(bm, d, W, n_txn, thr, node_cap, 0, out);
+    return orc_mine_fast_order(bm, d, W, n_txn, thr, node_cap, 0, NULL, out);
 }

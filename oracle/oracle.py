@@ -54,7 +54,7 @@ def lib():
         L.orc_mine_dfs.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_mine_fast.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_mine_fast_order.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int,
-                                          C.POINTER(_Mfis)]
+                                          C.POINTER(C.c_double), C.POINTER(_Mfis)]
         L.orc_mine_engine.argtypes = [u64p, C.c_uint32, C.c_uint64, C.c_uint32, u32p, C.c_uint32, C.c_uint64, C.POINTER(_Mfis)]
         L.orc_free.argtypes = [C.POINTER(_Mfis)]
         L.orc_online_bins.argtypes = [C.POINTER(C.c_double), C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
@@ -152,16 +152,20 @@ def mine_mfi(bm, n_txn, min_sup=0.05, min_count=None, node_cap=0):
     return _collect(m), nodes
 
 
-def mine_fast(bm, n_txn, thr, node_cap=0, order="support"):
+def mine_fast(bm, n_txn, thr, node_cap=0, order="support", key=None):
     """Pruned exact MFI miner (PEP/HUT/FHUT, projection): [(items, support)], nodes.
-    ``order``: "support" (each node's extensions in ascending support) or
-    "support_desc" (the reference's global descending-support order); the set
-    is the same, the number of nodes is not."""
+    ``order``: "support" (each node's extensions in ascending support),
+    "support_desc" (the reference's global descending-support order) or "key"
+    (one global order of ascending ``key[item]``); the set is the same, the
+    number of nodes is not."""
     bm = np.ascontiguousarray(bm, dtype=np.uint64)
     m = _Mfis()
-    code = {"support": 0, "support_desc": 1}[order]
+    code = {"support": 0, "support_desc": 1, "key": 2}[order]
+    kv = np.ascontiguousarray(key if key is not None else np.zeros(bm.shape[0]), dtype=np.float64)
+    if len(kv) < bm.shape[0]:
+        raise ValueError("key needs one value per bitmap row")
     rc = lib().orc_mine_fast_order(_p(bm, C.c_uint64), bm.shape[0], bm.shape[1], n_txn, max(1, int(thr)),
-                                   node_cap, code, C.byref(m))
+                                   node_cap, code, _p(kv, C.c_double), C.byref(m))
     nodes = int(m.nodes)
     if rc == 1:
         lib().orc_free(C.byref(m))
